@@ -1,0 +1,13 @@
+"""GB300 GP-MOOD: one FP64 SSP-RK3 step of GP-MOOD on one GPU.
+
+Package layout:
+  csrc/        CUDA kernels (sm_103a) and the C ABI of libgpmood.so
+  gpmood.py    ctypes binding mirroring the reference's time_stepping/Setdt/Boundary_C
+  ic.py        initial conditions of the benchmark problems
+  build.py     in-tree build of libgpmood.so
+"""
+from .gpmood import (DMR, FP_EXACT, FP_FAST, GP_MOOD, GP_SE, HLLC, NEUMANN, NGC, NN_GP_MOOD, PERIODIC,
+                     REFLECTIVE, SSP_RK3, GpmoodError, Params, Solver, default_params, load_library, padded)
+
+__all__ = ["DMR", "FP_EXACT", "FP_FAST", "GP_MOOD", "GP_SE", "HLLC", "NEUMANN", "NGC", "NN_GP_MOOD", "PERIODIC",
+           "REFLECTIVE", "SSP_RK3", "GpmoodError", "Params", "Solver", "default_params", "load_library", "padded"]

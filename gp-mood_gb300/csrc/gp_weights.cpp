@@ -1,0 +1,215 @@
+// gp_weights.cpp -- host precompute of the GP-SE reconstruction weights.
+//
+// Follows gp-mood-code/GP_init.f90:26-357 (GP_presim_sphere) and the
+// Cholesky inverse of gp-mood-code/linalg.f90:5-95, in IEEE binary128 like the
+// reference's real(16).  The weights are rounded to double once at the end,
+// exactly where the reference rounds (GP_init.f90:257, 267-268), and the
+// prediction weights are normalised to sum one in double (GP_init.f90:262).
+//
+// Squared-exponential kernel with length scale l; every quantity is an
+// integral of the kernel over unit cells, so all distances are in cells:
+//   covariance of two cell averages (GP_init.f90:459-511) and
+//   prediction vector of a point value at a face Gauss point (:446-455),
+//   second derivative at the cell centre (:431-443) for the U2 check.
+#define __STDC_WANT_IEC_60559_TYPES_EXT__
+#include <math.h>
+#include <string.h>
+
+#include "gpm_common.h"
+
+namespace {
+
+using f128 = _Float128;
+
+// Diamond ("sphere") stencil, nested by order: 1 point, +4 (radius 1), +8 (radius 2).
+// Ordering of gp-mood-code/GP_init.f90:97-138.
+const int kStencil[13][2] = {{0, 0},  {-1, 0}, {0, 1},  {1, 0},  {0, -1}, {-1, -1}, {-1, 1},
+                             {1, 1},  {1, -1}, {0, -2}, {-2, 0}, {0, 2},  {2, 0}};
+
+int stencil_size(int ord) { return ord == 1 ? 1 : (ord == 3 ? 5 : 13); }
+
+struct SeKernel {
+    f128 ell;       // physical length scale, ell_o_dx * min(dx, dy)
+    f128 hx, hy;    // cell sizes
+    f128 pi, inv_sqrt_pi, sqrt2;
+
+    // One factor of the cell-average covariance at separation d (cells), scale s = ell/h.
+    f128 cov1d(f128 d, f128 s) const {
+        const f128 a11 = (d + 1) / (sqrt2 * s);
+        const f128 a12 = (d - 1) / (sqrt2 * s);
+        const f128 a21 = -(((d + 1) * (d + 1)) / (2 * (s * s)));
+        const f128 a22 = -(((d - 1) * (d - 1)) / (2 * (s * s)));
+        const f128 a31 = d / (sqrt2 * s);
+        const f128 a32 = -(d * d) / (2 * (s * s));
+        return (sqrtf128(pi) * (s * s)) *
+               (a11 * erff128(a11) + a12 * erff128(a12) + inv_sqrt_pi * (expf128(a21) + expf128(a22)) -
+                2 * (a31 * erff128(a31) + inv_sqrt_pi * expf128(a32)));
+    }
+    f128 cov(f128 ddx, f128 ddy) const {
+        f128 r = cov1d(ddx, ell / hx);
+        return r * cov1d(ddy, ell / hy);
+    }
+    // Point value at offset d (cells) against the average of a unit cell.
+    f128 pred1d(f128 d, f128 h) const {
+        const f128 s = ell / h;
+        const f128 up = (d + (f128)1 / 2) / (sqrt2 * s);
+        const f128 dn = (d - (f128)1 / 2) / (sqrt2 * s);
+        return sqrtf128(pi / 2) * s * (erff128(up) - erff128(dn));
+    }
+    // Second derivative (physical units) of pred1d at the cell centre.
+    f128 pred1d_d2(f128 d, f128 h) const {
+        const f128 m = d - (f128)0.5, p = d + (f128)0.5, s = ell / h;
+        const f128 em = -(m * m) / (2 * (s * s));
+        const f128 ep = -(p * p) / (2 * (s * s));
+        return ((f128)1 / (ell * ell)) * (m * expf128(em) - p * expf128(ep));
+    }
+};
+
+// Inverse of a symmetric positive definite matrix by Cholesky: A = L L^T, then
+// one forward and one backward substitution per unit vector (linalg.f90:78-95).
+void spd_inverse(const f128* a, f128* inv, int n) {
+    f128 L[13][13] = {};
+    for (int i = 0; i < n; i++) {
+        f128 acc = 0;
+        for (int k = 0; k < i; k++) acc = acc + L[i][k] * L[i][k];
+        L[i][i] = sqrtf128(a[i * n + i] - acc);
+        for (int j = i + 1; j < n; j++) {
+            acc = 0;
+            for (int k = 0; k < i; k++) acc = acc + L[i][k] * L[j][k];
+            L[j][i] = (a[j * n + i] - acc) / L[i][i];
+        }
+    }
+    for (int col = 0; col < n; col++) {
+        f128 y[13], x[13];
+        for (int i = 0; i < n; i++) {
+            f128 acc = 0;
+            for (int j = 0; j < i; j++) acc = acc + L[i][j] * y[j];
+            y[i] = ((i == col ? (f128)1 : (f128)0) - acc) / L[i][i];
+        }
+        for (int i = n - 1; i >= 0; i--) {
+            f128 acc = 0;
+            for (int j = i + 1; j < n; j++) acc = acc + L[j][i] * x[j];
+            x[i] = (y[i] - acc) / L[i][i];
+        }
+        for (int i = 0; i < n; i++) inv[col * n + i] = x[i];
+    }
+}
+
+// Gauss-Legendre points on [-1/2, 1/2] and weights summing to one
+// (GP_init.f90:45-83): rules up to 3 points are binary128 expressions, the
+// 4- and 5-point rules are double expressions, as in the reference.
+void gauss_rule(int ngp, f128* pt, double* w) {
+    const f128 s3 = sqrtf128((f128)3), s35 = sqrtf128((f128)3 / 5);
+    const double s65 = sqrt(6. / 5), s30 = sqrt(30.), s107 = sqrt(10. / 7), s70 = sqrt(70.);
+    const double third = 1. / 3;
+    if (ngp == 1) {
+        pt[0] = 0; w[0] = 1.0;
+    } else if (ngp == 2) {
+        pt[0] = -(f128)0.5 / s3; pt[1] = (f128)0.5 / s3;
+        w[0] = w[1] = 0.5;
+    } else if (ngp == 3) {
+        pt[0] = -(f128)0.5 * s35; pt[1] = 0; pt[2] = (f128)0.5 * s35;
+        w[0] = w[2] = 0.5 * 5. / 9;
+        w[1] = 0.5 * 8. / 9;
+    } else if (ngp == 4) {
+        const double inner = 0.5 * sqrt(3. / 7 - (2. / 7) * s65);
+        const double outer = 0.5 * sqrt(3. / 7 + (2. / 7) * s65);
+        pt[0] = -outer; pt[1] = -inner; pt[2] = inner; pt[3] = outer;
+        w[0] = w[3] = 0.5 * (1. / 36) * (18. - s30);
+        w[1] = w[2] = 0.5 * (1. / 36) * (18. + s30);
+    } else {
+        const double inner = 0.5 * third * sqrt(5. - 2 * s107);
+        const double outer = 0.5 * third * sqrt(5. + 2 * s107);
+        pt[0] = -outer; pt[1] = -inner; pt[2] = 0.; pt[3] = inner; pt[4] = outer;
+        w[0] = w[4] = 0.5 * (322. - 13 * s70) / 900;
+        w[1] = w[3] = 0.5 * (322. + 13 * s70) / 900;
+        w[2] = 0.5 * 128. / 225;
+    }
+}
+
+}  // namespace
+
+extern "C" int gpm_gp_presim(double ell_o_dx, double lx, double ly, int lf, int nf, int mord, int ngp,
+                             GpWeights* out, double inv_err[3]) {
+    if (!(mord == 1 || mord == 3 || mord == 5) || ngp < 1 || ngp > GPM_MAXGP || lf < 1 || nf < 1)
+        return -1;
+    memset(out, 0, sizeof(*out));
+    for (int o = 0; o < 3; o++) inv_err[o] = 0.0;
+
+    SeKernel k;
+    k.hx = (f128)lx / lf;
+    k.hy = (f128)ly / nf;
+    k.ell = (f128)ell_o_dx * (k.hx < k.hy ? k.hx : k.hy);
+    k.pi = 4 * atanf128((f128)1);
+    k.inv_sqrt_pi = (f128)1 / sqrtf128(k.pi);
+    k.sqrt2 = sqrtf128((f128)2);
+
+    f128 pts[GPM_MAXGP];
+    gauss_rule(ngp, pts, out->gw);
+
+    for (int ord = 1; ord <= mord; ord += 2) {
+        const int o = ord / 2, np = stencil_size(ord);
+        f128 K[13 * 13], Ki[13 * 13];
+        for (int a = 0; a < np; a++)
+            for (int b = 0; b < np; b++)
+                K[a * np + b] = k.cov((f128)(kStencil[a][0] - kStencil[b][0]),
+                                      (f128)(kStencil[a][1] - kStencil[b][1]));
+        spd_inverse(K, Ki, np);
+
+        f128 worst = 0;  // max |K Ki - I|, the GP_init.f90:250 self-check
+        for (int i = 0; i < np; i++)
+            for (int j = 0; j < np; j++) {
+                f128 s = 0;
+                for (int m = 0; m < np; m++) s = s + K[i * np + m] * Ki[m * np + j];
+                const f128 e = fabsf128(s - (i == j ? (f128)1 : (f128)0));
+                if (e > worst) worst = e;
+            }
+        inv_err[o] = (double)worst;
+
+        // Face centre offsets (cells) of faces iL, iT, iR, iB and the direction
+        // along which the Gauss points run (0 = along y, 1 = along x).
+        const f128 half = (f128)1 / 2;
+        const f128 fc[4][2] = {{-half, 0}, {0, half}, {half, 0}, {0, -half}};
+        const int along_x[4] = {0, 1, 0, 1};
+        for (int face = 0; face < 4; face++)
+            for (int g = 0; g < ngp; g++) {
+                const f128 px = along_x[face] ? pts[g] : fc[face][0];
+                const f128 py = along_x[face] ? fc[face][1] : pts[g];
+                f128 t[13];
+                for (int a = 0; a < np; a++) {
+                    t[a] = k.pred1d((f128)kStencil[a][0] - px, k.hx);
+                    t[a] = t[a] * k.pred1d((f128)kStencil[a][1] - py, k.hy);
+                }
+                double z[13];
+                for (int b = 0; b < np; b++) {
+                    f128 s = 0;
+                    for (int a = 0; a < np; a++) s = s + t[a] * Ki[a * np + b];
+                    z[b] = (double)s;
+                }
+                double sum = 0.0;
+                for (int b = 0; b < np; b++) sum = sum + z[b];
+                for (int b = 0; b < np; b++) out->zt[o][face][g][b] = z[b] / sum;
+            }
+
+        if (ord == 3) {
+            f128 dx2[5], dy2[5];
+            for (int a = 0; a < np; a++) {
+                const f128 ox = (f128)kStencil[a][0], oy = (f128)kStencil[a][1];
+                dx2[a] = k.pred1d_d2(ox, k.hx);
+                dx2[a] = dx2[a] * k.pred1d(oy, k.hy);
+                dy2[a] = k.pred1d_d2(oy, k.hy);
+                dy2[a] = dy2[a] * k.pred1d(ox, k.hx);
+            }
+            for (int b = 0; b < np; b++) {
+                f128 sx = 0, sy = 0;
+                for (int a = 0; a < np; a++) {
+                    sx = sx + dx2[a] * Ki[a * np + b];
+                    sy = sy + dy2[a] * Ki[a * np + b];
+                }
+                out->d2x[b] = (double)sx;
+                out->d2y[b] = (double)sy;
+            }
+        }
+    }
+    return 0;
+}

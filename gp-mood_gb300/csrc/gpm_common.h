@@ -1,0 +1,86 @@
+// gpm_common.h -- types shared by the GP-MOOD kernels and the C-ABI host code.
+//
+// Device layout (identical to the reference's U(4, lb:le, nb:ne)): one cell is
+// four consecutive doubles (rho, rho*u, rho*v, E); cells run x-fastest over the
+// padded grid of (lf+8) x (nf+8) cells, ngc = 4 ghost layers on every side.
+// Cell (l, n) with l in [-3, lf+4] sits at linear index (n+3)*nx + (l+3).
+//
+// Face fluxes are stored per cell index of the face's low side:
+//   Fx[ci(l,n)] = x-face between (l,n) and (l+1,n), l in [0,lf], n in [1,nf]
+//   Fy[ci(l,n)] = y-face between (l,n) and (l,n+1), l in [1,lf], n in [0,nf]
+// (the L_Flux_x / L_Flux_y of gp-mood-code/mod_FE.f90:30-31).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#define GPM_NGC 4
+#define GPM_MAXGP 5
+
+// GP weights of GP_presim_sphere (gp-mood-code/GP_init.f90:254-268), passed to
+// kernels by value so that they sit in the constant parameter bank.
+struct GpWeights {
+    double zt[3][4][GPM_MAXGP][13];  // [ord 1,3,5][face iL,iT,iR,iB][gauss pt][stencil pt]
+    double gw[GPM_MAXGP];            // gauss_weight(ngp, :)
+    double d2x[5], d2y[5];           // GP_d2x_sp(3,:), GP_d2y_sp(3,:)
+};
+
+struct GridGeom {
+    int lf, nf, nx, ny;  // interior sizes and padded sizes (nx = lf + 8)
+    double dx, dy;
+    int bc_type, ngp, mord, method;
+    int dmp, u2, u2_tol;
+    int pad;
+};
+
+// Scalars that stay on the device across a step.
+struct DevScalars {
+    double t, dt, qx, qy;             // time, step, dt/dx, dt/dy
+    double tmax, cfl;
+    unsigned long long dtmin_bits;    // Setdt reduction slot (bits of a positive double)
+    int ntrb[2];                      // troubled-cell counts, double-buffered lists
+    int status;                       // GPMOOD status bits
+    int pad;
+    unsigned long long detected_step; // count_detected_cell of the current step
+    unsigned long long apriori_step;
+};
+
+enum { GPM_STATUS_NAN = 1, GPM_STATUS_MOODCAP = 2, GPM_STATUS_DT = 4 };
+
+// Launch-time arguments of one RK stage.
+struct StageArgs {
+    GridGeom g;
+    const double* uin;     // stage input (BC applied)
+    double* uout;          // stage output
+    double* fx;            // face flux stores (4 doubles per face)
+    double* fy;
+    int8_t* order;         // CellGPO per padded cell
+    unsigned* stamp;       // per-cell pass stamps (dedup of the dirty set)
+    int* tlist[2];         // troubled-cell lists (padded linear indices)
+    DevScalars* sc;
+    int uniform_order;     // 1: every cell starts at mord (plain GP-MOOD)
+    int stage;             // 0, 1, 2 -> t_rk = t, t+dt, t+dt/2
+};
+
+// Host-side launchers implemented once per floating-point variant
+// (stage_kernels.cu compiled with and without FMA contraction).
+struct KernelTable {
+    void (*bc)(const GridGeom& g, double* u, const DevScalars* sc, int stage, cudaStream_t s);
+    void (*flux_all)(const StageArgs& a, const GpWeights& w, cudaStream_t s);
+    void (*update_detect)(const StageArgs& a, const GpWeights& w, int cur, cudaStream_t s);
+    void (*mood_mark)(const StageArgs& a, int cur, int max_trb, cudaStream_t s);
+    void (*mood_faces)(const StageArgs& a, const GpWeights& w, int cur, int max_trb, cudaStream_t s);
+    void (*mood_cells)(const StageArgs& a, const GpWeights& w, int cur, int max_trb, unsigned pass_id,
+                       cudaStream_t s);
+    void (*combine)(const GridGeom& g, const double* x, double* y, double a, double b, int with_cfl,
+                    DevScalars* sc, cudaStream_t s);
+    void (*cfl)(const GridGeom& g, const double* u, DevScalars* sc, cudaStream_t s);
+    void (*dt_finalize)(const GridGeom& g, DevScalars* sc, double dtfinal, cudaStream_t s);
+    void (*advance_t)(DevScalars* sc, cudaStream_t s);
+};
+
+namespace gpm_exact { extern const KernelTable table; }
+namespace gpm_fast { extern const KernelTable table; }
+
+// Host GP precompute (gp_weights.cpp).  Returns 0 or -1 on bad knobs.
+extern "C" int gpm_gp_presim(double ell_o_dx, double lx, double ly, int lf, int nf, int mord, int ngp,
+                             GpWeights* out, double inv_err[3]);

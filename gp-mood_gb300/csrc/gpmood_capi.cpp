@@ -1,0 +1,500 @@
+// gpmood_capi.cpp -- the C ABI of libgpmood.so (declared in include/gpmood.h).
+//
+// Host orchestration of one SSP-RK3 step on the device.  All arrays of a
+// context live in HBM for the context's lifetime; the only host<->device
+// traffic of a step is the caller's own state copy (host-buffer calls) and one
+// 4-byte troubled-cell count per MOOD pass.
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <string.h>
+
+#include <new>
+
+#include "../../include/gpmood.h"
+#include "gpm_common.h"
+#include "nn_gate.h"
+
+struct gpmood_ctx {
+    gpmood_params p;
+    GridGeom g;
+    GpWeights w;
+    double inv_err[3];
+    const KernelTable* kt;
+    cudaStream_t stream;
+    size_t ncell;                 // padded cells
+    double *dU, *dUr, *dU1, *dU2, *dFx, *dFy;
+    int8_t* dOrder;
+    unsigned* dStamp;
+    int* dList[2];
+    DevScalars* dSc;
+    DevScalars* hSc;              // pinned mirror
+    int* hCount;                  // pinned troubled count
+    unsigned pass_id;
+    double t;                     // host mirror of the time
+    int niter;
+    bool have_state;
+    bool dt_pending;              // dSc->dtmin_bits holds Setdt of dU
+    gpmood_counters ctr;
+    NnGate* nn;                   // a-priori gate (method 203), or null
+    char err[512];
+};
+
+namespace {
+
+thread_local char g_err[512];
+
+int fail(gpmood_ctx* c, int code, const char* fmt, ...) {
+    char* dst = c ? c->err : g_err;
+    va_list ap;
+    va_start(ap, fmt);
+    vsnprintf(dst, 512, fmt, ap);
+    va_end(ap);
+    if (c) memcpy(g_err, c->err, 512);
+    return code;
+}
+
+#define CU(call)                                                                                       \
+    do {                                                                                               \
+        cudaError_t e_ = (call);                                                                       \
+        if (e_ != cudaSuccess) return fail(c, GPMOOD_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+    } while (0)
+
+int check_launch(gpmood_ctx* c, const char* what) {
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return fail(c, GPMOOD_E_CUDA, "%s: %s", what, cudaGetErrorString(e));
+    return 0;
+}
+
+size_t state_bytes(const gpmood_ctx* c) { return c->ncell * 4 * sizeof(double); }
+
+StageArgs stage_args(gpmood_ctx* c, const double* uin, double* uout, int stage, bool uniform) {
+    StageArgs a;
+    a.g = c->g;
+    a.uin = uin;
+    a.uout = uout;
+    a.fx = c->dFx;
+    a.fy = c->dFy;
+    a.order = c->dOrder;
+    a.stamp = c->dStamp;
+    a.tlist[0] = c->dList[0];
+    a.tlist[1] = c->dList[1];
+    a.sc = c->dSc;
+    a.uniform_order = uniform ? 1 : 0;
+    a.stage = stage;
+    return a;
+}
+
+// One Forward_Euler stage (mod_FE.f90:20-190) from uin (device) into uout.
+int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* passes) {
+    cudaStream_t s = c->stream;
+    const KernelTable& kt = *c->kt;
+    c->kt->bc(c->g, uin, c->dSc, stage, s);  // Boundary_C(Uin), :64
+    bool uniform = true;
+    CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, s));  // CellGPO = mord, :48
+    if (c->p.method == GPMOOD_NN_GP_MOOD && c->nn && c->niter + 1 > c->p.nsteps_with_no_nn) {
+        int rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, s);  // :51-56
+        if (rc) return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
+        uniform = false;
+    }
+    CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), s));
+    StageArgs a = stage_args(c, uin, uout, stage, uniform);
+    kt.flux_all(a, c->w, s);
+    kt.update_detect(a, c->w, 0, s);
+    int rc = check_launch(c, "first MOOD pass");
+    if (rc) return rc;
+    long long npass = 1;
+    if (c->p.method == GPMOOD_GP_MOOD || c->p.method == GPMOOD_NN_GP_MOOD) {
+        int cur = 0;
+        for (;;) {
+            CU(cudaMemcpyAsync(c->hCount, &c->dSc->ntrb[cur], sizeof(int), cudaMemcpyDeviceToHost, s));
+            CU(cudaStreamSynchronize(s));
+            const int nt = *c->hCount;
+            if (nt == 0) break;  // MOOD_finished
+            if (npass >= c->p.max_mood_iters) {
+                c->ctr.status_flags |= GPM_STATUS_MOODCAP;
+                return fail(c, GPMOOD_E_MOOD_CAP, "MOOD loop did not converge in %d passes (%d troubled cells left)",
+                            c->p.max_mood_iters, nt);
+            }
+            npass++;
+            kt.mood_mark(a, cur, nt, s);
+            kt.mood_faces(a, c->w, cur, nt, s);
+            kt.mood_cells(a, c->w, cur, nt, ++c->pass_id, s);
+            rc = check_launch(c, "MOOD pass");
+            if (rc) return rc;
+            cur ^= 1;
+        }
+    }
+    kt.bc(c->g, uout, c->dSc, stage, s);  // the last DETECTION's Boundary_C(Uout)
+    *passes += npass;
+    if (npass > c->ctr.max_passes_stage) c->ctr.max_passes_stage = npass;
+    return check_launch(c, "stage");
+}
+
+// SSP_RK3_ (mod_SSP_RK3.f90:12-39) from u into ur; t, dt, qx, qy already on the
+// device.  with_cfl fuses the next step's Setdt into the final combination.
+int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
+    cudaStream_t s = c->stream;
+    long long passes = 0;
+    CU(cudaMemsetAsync(&c->dSc->detected_step, 0, 2 * sizeof(unsigned long long), s));
+    int rc = run_stage(c, u, c->dU1, 0, &passes);
+    if (rc) return rc;
+    rc = run_stage(c, c->dU1, c->dU2, 1, &passes);
+    if (rc) return rc;
+    c->kt->combine(c->g, u, c->dU2, 0.75, 0.25, 0, c->dSc, s);  // U2 = 0.75 Uin + 0.25 U2
+    rc = run_stage(c, c->dU2, ur, 2, &passes);
+    if (rc) return rc;
+    c->kt->combine(c->g, u, ur, 1. / 3, 2. / 3, with_cfl ? 1 : 0, c->dSc, s);  // Uout = Uin/3 + 2 Uout/3
+    rc = check_launch(c, "combine");
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(c->hSc, c->dSc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+    CU(cudaStreamSynchronize(s));
+    c->ctr.detected_last_step = (long long)c->hSc->detected_step;
+    c->ctr.a_priori_last_step = (long long)c->hSc->apriori_step;
+    c->ctr.detected_total += (long long)c->hSc->detected_step;
+    c->ctr.mood_passes_last_step = passes;
+    c->ctr.steps++;
+    c->ctr.status_flags |= c->hSc->status;
+    return 0;
+}
+
+// Put t, dt and dt/dx, dt/dy computed on the host (IEEE, same bits) on the device.
+int set_time(gpmood_ctx* c, double t, double dt) {
+    c->hSc->t = t;
+    c->hSc->dt = dt;
+    c->hSc->qx = dt / c->g.dx;
+    c->hSc->qy = dt / c->g.dy;
+    CU(cudaMemcpyAsync(c->dSc, c->hSc, 4 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    return 0;
+}
+
+int validate(const gpmood_params* p, char* why, size_t n) {
+    if (!p) { snprintf(why, n, "params is NULL"); return -1; }
+    if (p->integrator != GPMOOD_SSP_RK3) { snprintf(why, n, "integrator %d unsupported (only SSP_RK3=10)", p->integrator); return -1; }
+    if (p->method != GPMOOD_GP_MOOD && p->method != GPMOOD_GP_SE && p->method != GPMOOD_NN_GP_MOOD) {
+        snprintf(why, n, "method %d unsupported (GP_MOOD=2, GP_SE=202, NN_GP_MOOD=203)", p->method); return -1; }
+    if (p->num_flux != GPMOOD_HLLC) { snprintf(why, n, "numFlux %d unsupported (only HLLC=100)", p->num_flux); return -1; }
+    if (!(p->mord == 1 || p->mord == 3 || p->mord == 5)) { snprintf(why, n, "Mord %d unsupported (1, 3, 5)", p->mord); return -1; }
+    if (p->ngp < 1 || p->ngp > 5) { snprintf(why, n, "ngp %d out of 1..5", p->ngp); return -1; }
+    if (p->lf < 4 || p->nf < 4 || p->lf > 65536 || p->nf > 65536) { snprintf(why, n, "grid %dx%d out of range", p->lf, p->nf); return -1; }
+    if (p->bc_type != GPMOOD_NEUMANN && p->bc_type != GPMOOD_PERIODIC && p->bc_type != GPMOOD_REFLECTIVE &&
+        p->bc_type != GPMOOD_DMR) { snprintf(why, n, "BC_type %d unsupported", p->bc_type); return -1; }
+    if (!(p->cfl > 0) || !(p->lx > 0) || !(p->ly > 0) || !(p->ell_o_dx > 0)) { snprintf(why, n, "CFL, Lx, Ly, ell_o_dx must be > 0"); return -1; }
+    if (p->fp_mode != GPMOOD_FP_EXACT && p->fp_mode != GPMOOD_FP_FAST) { snprintf(why, n, "fp_mode %d unknown", p->fp_mode); return -1; }
+    if (p->max_mood_iters < 1) { snprintf(why, n, "max_mood_iters must be >= 1"); return -1; }
+    return 0;
+}
+
+void free_all(gpmood_ctx* c) {
+    if (!c) return;
+    cudaFree(c->dU); cudaFree(c->dUr); cudaFree(c->dU1); cudaFree(c->dU2);
+    cudaFree(c->dFx); cudaFree(c->dFy); cudaFree(c->dOrder); cudaFree(c->dStamp);
+    cudaFree(c->dList[0]); cudaFree(c->dList[1]); cudaFree(c->dSc);
+    if (c->hSc) cudaFreeHost(c->hSc);
+    if (c->hCount) cudaFreeHost(c->hCount);
+    if (c->nn) nn_gate_destroy(c->nn);
+    if (c->stream) cudaStreamDestroy(c->stream);
+}
+
+}  // namespace
+
+extern "C" {
+
+int gpmood_default_params(gpmood_params* p) {
+    if (!p) return fail(nullptr, GPMOOD_E_ARG, "params is NULL");
+    memset(p, 0, sizeof(*p));
+    p->cfl = 0.8;
+    p->ell_o_dx = 12.0;
+    p->lx = 1.0;
+    p->ly = 1.0;
+    p->tmax = 0.8;
+    p->integrator = GPMOOD_SSP_RK3;
+    p->method = GPMOOD_GP_MOOD;
+    p->mord = 5;
+    p->ngp = 3;
+    p->dmp = p->u2 = p->u2_tol = 1;
+    p->num_flux = GPMOOD_HLLC;
+    p->lf = p->nf = 256;
+    p->bc_type = GPMOOD_NEUMANN;
+    p->nmax = 1 << 30;
+    p->fp_mode = GPMOOD_FP_EXACT;
+    p->max_mood_iters = 64;
+    p->nsteps_with_no_nn = 0;
+    return 0;
+}
+
+int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
+    gpmood_ctx* c = nullptr;
+    if (!out) return fail(nullptr, GPMOOD_E_ARG, "out is NULL");
+    *out = nullptr;
+    char why[256];
+    if (validate(p, why, sizeof why)) return fail(nullptr, GPMOOD_E_ARG, "%s", why);
+    c = new (std::nothrow) gpmood_ctx();
+    if (!c) return fail(nullptr, GPMOOD_E_ARG, "out of host memory");
+    c->p = *p;
+    c->g.lf = p->lf;
+    c->g.nf = p->nf;
+    c->g.nx = p->lf + 2 * GPM_NGC;
+    c->g.ny = p->nf + 2 * GPM_NGC;
+    // dx = real(Lx_16/lf, PR) (global_variables.f90:86-88), rounded from binary128.
+    c->g.dx = (double)((_Float128)p->lx / p->lf);
+    c->g.dy = (double)((_Float128)p->ly / p->nf);
+    c->g.bc_type = p->bc_type;
+    c->g.ngp = p->ngp;
+    c->g.mord = p->mord;
+    c->g.method = p->method;
+    c->g.dmp = p->dmp;
+    c->g.u2 = p->u2;
+    c->g.u2_tol = p->u2_tol;
+    c->ncell = (size_t)c->g.nx * c->g.ny;
+    c->kt = p->fp_mode == GPMOOD_FP_FAST ? &gpm_fast::table : &gpm_exact::table;
+    if (gpm_gp_presim(p->ell_o_dx, p->lx, p->ly, p->lf, p->nf, p->mord, p->ngp, &c->w, c->inv_err)) {
+        delete c;
+        return fail(nullptr, GPMOOD_E_ARG, "GP precompute rejected the knobs");
+    }
+    int ndev = 0;
+    cudaError_t e = cudaGetDeviceCount(&ndev);
+    if (e != cudaSuccess || ndev < 1) {
+        delete c;
+        return fail(nullptr, GPMOOD_E_CUDA, "no CUDA device: %s", cudaGetErrorString(e));
+    }
+#define ALLOC(ptr, bytes)                                                                             \
+    do {                                                                                              \
+        cudaError_t e_ = cudaMalloc((void**)&(ptr), (bytes));                                         \
+        if (e_ != cudaSuccess) {                                                                      \
+            fail(c, GPMOOD_E_CUDA, "cudaMalloc(%zu): %s", (size_t)(bytes), cudaGetErrorString(e_));   \
+            free_all(c);                                                                              \
+            delete c;                                                                                 \
+            return GPMOOD_E_CUDA;                                                                     \
+        }                                                                                             \
+    } while (0)
+    const size_t sb = c->ncell * 4 * sizeof(double);
+    ALLOC(c->dU, sb);
+    ALLOC(c->dUr, sb);
+    ALLOC(c->dU1, sb);
+    ALLOC(c->dU2, sb);
+    ALLOC(c->dFx, sb);
+    ALLOC(c->dFy, sb);
+    ALLOC(c->dOrder, c->ncell);
+    ALLOC(c->dStamp, c->ncell * sizeof(unsigned));
+    ALLOC(c->dList[0], c->ncell * sizeof(int));
+    ALLOC(c->dList[1], c->ncell * sizeof(int));
+    ALLOC(c->dSc, sizeof(DevScalars));
+#undef ALLOC
+    if (cudaMallocHost((void**)&c->hSc, sizeof(DevScalars)) != cudaSuccess ||
+        cudaMallocHost((void**)&c->hCount, sizeof(int)) != cudaSuccess ||
+        cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
+        fail(c, GPMOOD_E_CUDA, "pinned memory / stream creation failed");
+        free_all(c);
+        delete c;
+        return GPMOOD_E_CUDA;
+    }
+    memset(c->hSc, 0, sizeof(DevScalars));
+    c->hSc->tmax = p->tmax;
+    c->hSc->cfl = p->cfl;
+    c->hSc->dtmin_bits = 0x46293e5939a08ceaULL;  // bits of 1.0e30
+    if (cudaMemcpy(c->dSc, c->hSc, sizeof(DevScalars), cudaMemcpyHostToDevice) != cudaSuccess ||
+        cudaMemset(c->dStamp, 0, c->ncell * sizeof(unsigned)) != cudaSuccess ||
+        cudaMemset(c->dFx, 0, sb) != cudaSuccess || cudaMemset(c->dFy, 0, sb) != cudaSuccess ||
+        cudaMemset(c->dU, 0, sb) != cudaSuccess || cudaMemset(c->dUr, 0, sb) != cudaSuccess ||
+        cudaMemset(c->dU1, 0, sb) != cudaSuccess || cudaMemset(c->dU2, 0, sb) != cudaSuccess) {
+        fail(c, GPMOOD_E_CUDA, "device initialisation failed");
+        free_all(c);
+        delete c;
+        return GPMOOD_E_CUDA;
+    }
+    if (p->method == GPMOOD_NN_GP_MOOD) {
+        c->nn = nn_gate_create(c->g);
+        if (!c->nn) {
+            fail(c, GPMOOD_E_CUDA, "NN gate allocation failed");
+            free_all(c);
+            delete c;
+            return GPMOOD_E_CUDA;
+        }
+    }
+    *out = c;
+    return 0;
+}
+
+void gpmood_destroy(gpmood_ctx* c) {
+    if (!c) return;
+    cudaStreamSynchronize(c->stream);
+    free_all(c);
+    delete c;
+}
+
+int gpmood_last_error(const gpmood_ctx* c, char* buf, int len) {
+    if (!buf || len <= 0) return GPMOOD_E_ARG;
+    snprintf(buf, (size_t)len, "%s", c ? c->err : g_err);
+    return 0;
+}
+
+int gpmood_get_weights(const gpmood_ctx* c, double* zt, double* d2, double* inv_err) {
+    if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
+    const int ngp = c->p.ngp;
+    if (zt)
+        for (int o = 0; o < 3; o++)
+            for (int f = 0; f < 4; f++)
+                for (int g = 0; g < ngp; g++)
+                    for (int m = 0; m < 13; m++) zt[((o * 4 + f) * ngp + g) * 13 + m] = c->w.zt[o][f][g][m];
+    if (d2)
+        for (int m = 0; m < 5; m++) {
+            d2[m] = c->w.d2x[m];
+            d2[5 + m] = c->w.d2y[m];
+        }
+    if (inv_err)
+        for (int o = 0; o < 3; o++) inv_err[o] = c->inv_err[o];
+    return 0;
+}
+
+int gpmood_gp_weights(const gpmood_params* p, double* zt, double* d2, double* inv_err) {
+    char why[256];
+    if (validate(p, why, sizeof why)) return fail(nullptr, GPMOOD_E_ARG, "%s", why);
+    GpWeights w;
+    double ie[3];
+    if (gpm_gp_presim(p->ell_o_dx, p->lx, p->ly, p->lf, p->nf, p->mord, p->ngp, &w, ie))
+        return fail(nullptr, GPMOOD_E_ARG, "GP precompute rejected the knobs");
+    const int ngp = p->ngp;
+    if (zt)
+        for (int o = 0; o < 3; o++)
+            for (int f = 0; f < 4; f++)
+                for (int g = 0; g < ngp; g++)
+                    for (int m = 0; m < 13; m++) zt[((o * 4 + f) * ngp + g) * 13 + m] = w.zt[o][f][g][m];
+    if (d2)
+        for (int m = 0; m < 5; m++) {
+            d2[m] = w.d2x[m];
+            d2[5 + m] = w.d2y[m];
+        }
+    if (inv_err)
+        for (int o = 0; o < 3; o++) inv_err[o] = ie[o];
+    return 0;
+}
+
+int gpmood_boundary_c(gpmood_ctx* c, double* u_host, double t_rk) {
+    if (!c || !u_host) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    CU(cudaMemcpyAsync(c->dU2, u_host, state_bytes(c), cudaMemcpyHostToDevice, c->stream));
+    int rc = set_time(c, t_rk, 0.0);
+    if (rc) return rc;
+    c->kt->bc(c->g, c->dU2, c->dSc, 0, c->stream);
+    rc = check_launch(c, "Boundary_C");
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(u_host, c->dU2, state_bytes(c), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int gpmood_setdt(gpmood_ctx* c, const double* u_host, double dtfinal, double* dt_out) {
+    if (!c || !u_host || !dt_out) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    CU(cudaMemcpyAsync(c->dU2, u_host, state_bytes(c), cudaMemcpyHostToDevice, c->stream));
+    c->kt->cfl(c->g, c->dU2, c->dSc, c->stream);
+    c->kt->dt_finalize(c->g, c->dSc, dtfinal < 0.0 ? 0.0 : dtfinal, c->stream);
+    int rc = check_launch(c, "Setdt");
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(c->hSc, c->dSc, sizeof(DevScalars), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    *dt_out = c->hSc->dt;
+    c->dt_pending = false;
+    if (c->hSc->status & GPM_STATUS_DT) return fail(c, GPMOOD_E_DT, "Setdt produced dt = %g", c->hSc->dt);
+    return 0;
+}
+
+int gpmood_time_stepping(gpmood_ctx* c, const double* uin_host, double* uout_host, double t, double dt) {
+    if (!c || !uin_host || !uout_host) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    if (!(dt > 0) || !isfinite(dt)) return fail(c, GPMOOD_E_DT, "dt = %g", dt);
+    CU(cudaMemcpyAsync(c->dU, uin_host, state_bytes(c), cudaMemcpyHostToDevice, c->stream));
+    int rc = set_time(c, t, dt);
+    if (rc) return rc;
+    rc = run_step(c, c->dU, c->dUr, false);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(uout_host, c->dUr, state_bytes(c), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    c->have_state = false;  // dU no longer mirrors a set_state upload
+    return 0;
+}
+
+int gpmood_time_stepping_dev(gpmood_ctx* c, double* d_uin, double* d_uout, double t, double dt) {
+    if (!c || !d_uin || !d_uout) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    if (!(dt > 0) || !isfinite(dt)) return fail(c, GPMOOD_E_DT, "dt = %g", dt);
+    int rc = set_time(c, t, dt);
+    if (rc) return rc;
+    return run_step(c, d_uin, d_uout, false);
+}
+
+int gpmood_set_state(gpmood_ctx* c, const double* u_host, double t) {
+    if (!c || !u_host) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    CU(cudaMemcpyAsync(c->dU, u_host, state_bytes(c), cudaMemcpyHostToDevice, c->stream));
+    int rc = set_time(c, t, 0.0);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    c->t = t;
+    c->niter = 0;
+    c->have_state = true;
+    c->dt_pending = false;
+    return 0;
+}
+
+int gpmood_get_state(gpmood_ctx* c, double* u_host, double* t, int* niter) {
+    if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
+    if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
+    if (u_host) {
+        CU(cudaMemcpyAsync(u_host, c->dU, state_bytes(c), cudaMemcpyDeviceToHost, c->stream));
+        CU(cudaStreamSynchronize(c->stream));
+    }
+    if (t) *t = c->t;
+    if (niter) *niter = c->niter;
+    return 0;
+}
+
+int gpmood_get_orders(gpmood_ctx* c, signed char* orders) {
+    if (!c || !orders) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    // CellGPO(1:lf, 1:nf): interior rows of the padded order array.
+    CU(cudaMemcpy2DAsync(orders, (size_t)c->p.lf, c->dOrder + (size_t)(GPM_NGC) * c->g.nx + GPM_NGC,
+                         (size_t)c->g.nx, (size_t)c->p.lf, (size_t)c->p.nf, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int gpmood_advance(gpmood_ctx* c, int nsteps, int* steps_done) {
+    if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
+    if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
+    if (steps_done) *steps_done = 0;
+    int done = 0;
+    while (done < nsteps && c->t < c->p.tmax && c->niter < c->p.nmax) {  // main.f90:145
+        if (!c->dt_pending) {  // Setdt(U) (main.f90:151); later steps fuse it into the last combine
+            c->kt->cfl(c->g, c->dU, c->dSc, c->stream);
+        }
+        c->kt->dt_finalize(c->g, c->dSc, -1.0, c->stream);
+        int rc = run_step(c, c->dU, c->dUr, true);
+        if (rc) return rc;
+        if (c->hSc->status & GPM_STATUS_DT) return fail(c, GPMOOD_E_DT, "Setdt produced dt = %g", c->hSc->dt);
+        c->kt->advance_t(c->dSc, c->stream);  // t = t + dt
+        double* tmp = c->dU;                   // U = Ur
+        c->dU = c->dUr;
+        c->dUr = tmp;
+        c->t = c->hSc->t + c->hSc->dt;
+        c->niter++;
+        c->dt_pending = true;
+        done++;
+        if (steps_done) *steps_done = done;
+    }
+    CU(cudaStreamSynchronize(c->stream));
+    return check_launch(c, "advance");
+}
+
+int gpmood_get_counters(const gpmood_ctx* c, gpmood_counters* out) {
+    if (!c || !out) return fail(nullptr, GPMOOD_E_ARG, "NULL argument");
+    *out = c->ctr;
+    return 0;
+}
+
+int gpmood_set_nn(gpmood_ctx* c, const float* params, int n) {
+    if (!c || !params) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    if (!c->nn) return fail(c, GPMOOD_E_STATE, "context was not created with method NN_GP_MOOD (203)");
+    if (n != NN_GATE_NPARAMS) return fail(c, GPMOOD_E_ARG, "expected %d gate parameters, got %d", NN_GATE_NPARAMS, n);
+    if (nn_gate_set(c->nn, params, c->stream)) return fail(c, GPMOOD_E_CUDA, "NN gate upload failed");
+    CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,282 @@
+// physics.cuh -- device physics of the GP-MOOD step: pressure, HLLC, GP dot
+// products, MOOD detection.  Included by stage_kernels.cu, which is compiled
+// twice: GPM_EXACT=1 with --fmad=false (every expression rounds exactly like
+// the reference's x86-64 build) and GPM_EXACT=0 with FMA contraction and
+// reciprocal reuse.
+//
+// Reference routines: physics.f90:9-75,132-143 (Flux, c2p_local, pressure),
+// mod_HLLC.f90:11-169 (HLLC_Flux), mod_GP_MOOD.f90:58-65 (dot products),
+// mod_subroutine_MOOD.f90:41-131,191-238 (DETECTION checks, shock_detector).
+#pragma once
+#include "gpm_common.h"
+
+#ifndef GPM_EXACT
+#error "GPM_EXACT must be defined"
+#endif
+
+#define GPM_GAMMA 1.4
+
+struct __align__(32) Cell {
+    double r, mx, my, e;
+};
+
+__device__ __forceinline__ Cell ld_cell(const double* p) {
+    const double2 a = __ldg(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldg(reinterpret_cast<const double2*>(p) + 1);
+    return Cell{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ Cell ld_cell_cg(const double* p) {  // data written earlier in the same kernel chain
+    const double2 a = __ldcg(reinterpret_cast<const double2*>(p));
+    const double2 b = __ldcg(reinterpret_cast<const double2*>(p) + 1);
+    return Cell{a.x, a.y, b.x, b.y};
+}
+__device__ __forceinline__ void st_cell(double* p, const Cell& c) {
+    reinterpret_cast<double2*>(p)[0] = make_double2(c.r, c.mx);
+    reinterpret_cast<double2*>(p)[1] = make_double2(c.my, c.e);
+}
+
+// x + 0.0 without an FP64 instruction.  A dot product written as
+// 0 + p1 + p2 + ... (Fortran dot_product) differs from p1 + p2 + ... only by
+// the sign of an exact zero result, so applying this at the end restores it.
+__device__ __forceinline__ double plus_zero(double x) {
+    return (__double_as_longlong(x) == (long long)0x8000000000000000ULL) ? 0.0 : x;
+}
+
+// Sign/NaN tests on the bit pattern (integer pipe, exact).
+__device__ __forceinline__ bool is_nan(double x) {
+    return (__double_as_longlong(x) & 0x7fffffffffffffffLL) > 0x7ff0000000000000LL;
+}
+// (x <= 0) .or. ISNAN(x): a non-positive double has a non-positive signed bit
+// pattern; a NaN with the sign bit set also does, and is caught either way.
+__device__ __forceinline__ bool le_zero_or_nan(double x) {
+    return (__double_as_longlong(x) <= 0LL) || is_nan(x);
+}
+
+// pressure(u), physics.f90:132-143: (y-1)*(E - 0.5*(mx^2+my^2)/rho)
+__device__ __forceinline__ double pressure(const Cell& u) {
+    return (GPM_GAMMA - 1.) * (u.e - (0.5 * (u.mx * u.mx + u.my * u.my) / u.r));
+}
+
+// Stencil offsets of the diamond stencil, GP_init.f90:97-138 ordering.
+__host__ __device__ constexpr int st_ox(int m) {
+    return m == 0 ? 0 : m == 1 ? -1 : m == 2 ? 0 : m == 3 ? 1 : m == 4 ? 0 : m == 5 ? -1 : m == 6 ? -1
+         : m == 7 ? 1 : m == 8 ? 1 : m == 9 ? 0 : m == 10 ? -2 : m == 11 ? 0 : 2;
+}
+__host__ __device__ constexpr int st_oy(int m) {
+    return m == 0 ? 0 : m == 1 ? 0 : m == 2 ? 1 : m == 3 ? 0 : m == 4 ? -1 : m == 5 ? -1 : m == 6 ? 1
+         : m == 7 ? 1 : m == 8 ? -1 : m == 9 ? -2 : m == 10 ? 0 : m == 11 ? 2 : 0;
+}
+__host__ __device__ constexpr int np_of(int ord) { return ord == 1 ? 1 : (ord == 3 ? 5 : 13); }
+
+// GP reconstruction of one face of one cell at NGP Gauss points:
+// u[g][k] = sum_m zt[g][m] * q[m][k], sequential in m (mod_GP_MOOD.f90:61).
+template <int NP, int NGP>
+__device__ __forceinline__ void gp_recon(const double* __restrict__ zface, const Cell* q, double (*u)[4]) {
+#pragma unroll
+    for (int g = 0; g < NGP; g++) {
+        const double* z = zface + g * 13;
+        double s0 = z[0] * q[0].r, s1 = z[0] * q[0].mx, s2 = z[0] * q[0].my, s3 = z[0] * q[0].e;
+#pragma unroll
+        for (int m = 1; m < NP; m++) {
+            const double zm = z[m];
+            s0 = s0 + zm * q[m].r;
+            s1 = s1 + zm * q[m].mx;
+            s2 = s2 + zm * q[m].my;
+            s3 = s3 + zm * q[m].e;
+        }
+#if GPM_EXACT
+        u[g][0] = plus_zero(s0); u[g][1] = plus_zero(s1); u[g][2] = plus_zero(s2); u[g][3] = plus_zero(s3);
+#else
+        u[g][0] = s0; u[g][1] = s1; u[g][2] = s2; u[g][3] = s3;
+#endif
+    }
+}
+
+// Primitive recovery of one face state, c2p_local (physics.f90:51-75): normal
+// velocity vn, tangential velocity vt, vn^2, pressure, sound speed, admissibility.
+struct Prim {
+    double vn, vt, vn2, p, c;
+    bool adm;
+    double vx;  // x-velocity, needed for the 1/(vx-vx) of an inadmissible state
+#if !GPM_EXACT
+    double ir;  // 1/rho
+#endif
+};
+
+template <int DIR>
+__device__ __forceinline__ Prim c2p(const double* u) {
+    Prim s;
+#if GPM_EXACT
+    const double vx = u[1] / u[0];
+    const double vy = u[2] / u[0];
+    s.p = (GPM_GAMMA - 1.) * (u[3] - (0.5 * (u[1] * u[1] + u[2] * u[2]) / u[0]));
+    s.c = sqrt(GPM_GAMMA * s.p / u[0]);
+#else
+    const double ir = 1.0 / u[0];
+    const double vx = u[1] * ir;
+    const double vy = u[2] * ir;
+    s.p = (GPM_GAMMA - 1.) * (u[3] - 0.5 * (u[1] * vx + u[2] * vy));
+    s.c = sqrt(GPM_GAMMA * s.p * ir);
+    s.ir = ir;
+#endif
+    s.vx = vx;
+    s.vn = DIR == 0 ? vx : vy;
+    s.vt = DIR == 0 ? vy : vx;
+    s.vn2 = s.vn * s.vn;
+    s.adm = !(le_zero_or_nan(u[0]) || le_zero_or_nan(s.p));
+    return s;
+}
+
+// Physical flux F(u) in direction DIR, physics.f90:9-48 (admissible branch).
+template <int DIR>
+__device__ __forceinline__ void phys_flux(const double* u, const Prim& s, double* r) {
+    if (DIR == 0) {
+        r[0] = u[1];
+        r[1] = u[0] * s.vn2 + s.p;
+        r[2] = u[2] * s.vn;
+        r[3] = s.vn * (u[3] + s.p);
+    } else {
+        r[0] = u[2];
+        r[1] = u[1] * s.vn;
+        r[2] = u[0] * s.vn2 + s.p;
+        r[3] = s.vn * (u[3] + s.p);
+    }
+}
+
+// HLLC_Flux, mod_HLLC.f90:11-169, with the symmetry-preserving u* (:121-123).
+// Only the branch that the reference finally selects is evaluated; every
+// skipped quantity is unused by that branch, so the result is unchanged.
+template <int DIR>
+__device__ __forceinline__ void hllc(const double* ul, const double* ur, double* F) {
+    const Prim L = c2p<DIR>(ul);
+    const Prim R = c2p<DIR>(ur);
+    const double SL = fmin(L.vn - L.c, R.vn - R.c);
+    const double SR = fmax(L.vn + L.c, R.vn + R.c);
+    if (!(L.adm && R.adm)) {  // :166
+        const double bad = 1. / (R.vx - R.vx);
+        F[0] = F[1] = F[2] = F[3] = bad;
+        return;
+    }
+    if (SL >= 0.) {
+        phys_flux<DIR>(ul, L, F);
+        return;
+    }
+    const double numerL = SL - L.vn, numerR = SR - R.vn;
+    double uStar = ul[0] * L.vn * numerL - ur[0] * R.vn * numerR;
+    uStar = (R.p - L.p) + uStar;
+    const double aL = ul[0] * numerL, aR = ur[0] * numerR;
+    uStar = uStar / (aL - aR);
+    const bool left = (SL < 0.) && (uStar >= 0.);
+    const bool right = (uStar < 0.) && (SR >= 0.);
+    if (!left && !right) {
+        phys_flux<DIR>(ur, R, F);
+        return;
+    }
+    const double* u = left ? ul : ur;
+    const Prim& s = left ? L : R;
+    const double S = left ? SL : SR;
+    const double a = left ? aL : aR;
+    double Fk[4];
+    phys_flux<DIR>(u, s, Fk);
+    double st[4];
+    st[0] = 1.;
+    st[DIR == 0 ? 1 : 2] = uStar;
+    st[DIR == 0 ? 2 : 1] = s.vt;
+#if GPM_EXACT
+    const double dStar = a / (S - uStar);
+    st[3] = u[3] / u[0] + (uStar - s.vn) * (uStar + s.p / a);
+#else
+    const double den = S - uStar;
+    const double inv = 1.0 / (a * den);  // one division for a/den and p/a
+    const double dStar = a * a * inv;
+    st[3] = u[3] * s.ir + (uStar - s.vn) * (uStar + s.p * den * inv);
+#endif
+#pragma unroll
+    for (int k = 0; k < 4; k++) F[k] = Fk[k] + S * (st[k] * dStar - u[k]);
+}
+
+// Face flux with Gauss quadrature, mod_FE.f90:80-98: sum_g Fg*w_g from zero.
+template <int DIR, int NGP>
+__device__ __forceinline__ void quad_flux(const double (*uL)[4], const double (*uR)[4], const double* gw, double* F) {
+    double acc[4];
+#pragma unroll
+    for (int g = 0; g < NGP; g++) {
+        double Fg[4];
+        hllc<DIR>(uL[g], uR[g], Fg);
+#pragma unroll
+        for (int k = 0; k < 4; k++) acc[k] = (g == 0) ? Fg[k] * gw[0] : acc[k] + Fg[k] * gw[g];
+    }
+#if GPM_EXACT
+#pragma unroll
+    for (int k = 0; k < 4; k++) F[k] = plus_zero(acc[k]);
+#else
+#pragma unroll
+    for (int k = 0; k < 4; k++) F[k] = acc[k];
+#endif
+}
+
+// shock_detector, mod_subroutine_MOOD.f90:191-238, on Uin around (l, n).
+__device__ __forceinline__ bool shock_detector(const Cell& c, const Cell& L, const Cell& R, const Cell& B,
+                                               const Cell& T, double dx, double dy) {
+    double divV = (R.mx - L.mx) / dx + (T.my - B.my) / dy;
+    divV = 0.5 * divV / c.r;
+    divV = divV - 0.5 * (c.mx * (R.r - L.r) / dx + c.my * (T.r - B.r) / dy) / (c.r * c.r);
+    const double Ca = 1.4 * pressure(c) / c.r;
+    double Mach = (c.mx * c.mx + c.my * c.my) / (c.r * c.r);
+    Mach = sqrt(Mach / Ca);
+    const double pL = pressure(L), pR = pressure(R), pB = pressure(B), pT = pressure(T);
+    const double gradP = 0.5 * (fabs(pR - pL) / fmin(pL, pR) / dx + fabs(pT - pB) / fmin(pB, pT) / dy);
+    const double m = fmax(dx, dy);
+    return (divV < -(m * m)) && (Mach > 0.2) && (gradP > 5.0);
+}
+
+// DETECTION checks for one interior cell (mod_subroutine_MOOD.f90:41-131).
+// uin points at Uin(1, l, n) of a padded array of row pitch 4*nx doubles.
+// The DMP bounds test runs before the shock detector: both are side-effect
+// free and combined by .and., so the decision is the reference's.
+__device__ __forceinline__ bool mood_troubled(const Cell& uo, const double* __restrict__ uin, int nx,
+                                              const GridGeom& g, const double* d2x, const double* d2y) {
+    if (le_zero_or_nan(uo.r)) return true;
+    const double p = pressure(uo);
+    if (le_zero_or_nan(p)) return true;
+    if (!g.dmp) return false;
+    const size_t row = (size_t)4 * nx;
+    const Cell C = ld_cell(uin), Lc = ld_cell(uin - 4), Rc = ld_cell(uin + 4);
+    const Cell Bc = ld_cell(uin - row), Tc = ld_cell(uin + row);
+    const double mn = fmin(fmin(fmin(fmin(C.r, Lc.r), Bc.r), Tc.r), Rc.r);
+    const double mx = fmax(fmax(fmax(fmax(C.r, Lc.r), Bc.r), Tc.r), Rc.r);
+    const double Mm = mx - mn;
+    if (!(Mm > g.dx * g.dx * g.dx)) return false;                 // plateau, :68
+    if (!((uo.r > mx) || (uo.r < mn))) return false;              // :70
+    if (!shock_detector(C, Lc, Rc, Bc, Tc, g.dx, g.dy)) return false;
+    if (!g.u2) return true;
+    // U2 smooth-extremum test, :74-119: GP second derivatives of rho at the
+    // 5 cross cells, each from that cell's own 5-point cross.
+    double D2x[5], D2y[5];
+    const int ci_[5] = {-1, 0, 1, 0, 0}, cj_[5] = {0, 0, 0, -1, 1};  // (-1,0),(0,0),(1,0),(0,-1),(0,1)
+#pragma unroll
+    for (int s = 0; s < 5; s++) {
+        const double* base = uin + (ptrdiff_t)4 * ci_[s] + (ptrdiff_t)row * cj_[s];
+        double q[5];
+#pragma unroll
+        for (int k = 0; k < 5; k++) q[k] = __ldg(base + (ptrdiff_t)4 * st_ox(k) + (ptrdiff_t)row * st_oy(k));
+        double sx = d2x[0] * q[0], sy = d2y[0] * q[0];
+#pragma unroll
+        for (int k = 1; k < 5; k++) {
+            sx = sx + d2x[k] * q[k];
+            sy = sy + d2y[k] * q[k];
+        }
+        D2x[s] = sx;
+        D2y[s] = sy;
+    }
+    const double Xmin = fmin(fmin(fmin(fmin(D2x[0], D2x[1]), D2x[2]), D2x[3]), D2x[4]);
+    const double Xmax = fmax(fmax(fmax(fmax(D2x[0], D2x[1]), D2x[2]), D2x[3]), D2x[4]);
+    const double Ymin = fmin(fmin(fmin(fmin(D2y[0], D2y[1]), D2y[2]), D2y[3]), D2y[4]);
+    const double Ymax = fmax(fmax(fmax(fmax(D2y[0], D2y[1]), D2y[2]), D2y[3]), D2y[4]);
+    const double delta = g.u2_tol ? fmax(g.dx, g.dy) : 0.0;
+    if ((Xmin * Xmax > -delta) && ((fmax(fabs(Xmin), fabs(Xmax)) < delta) || (fabs(Xmin / Xmax) >= 1. / 2)))
+        return false;
+    if ((Ymin * Ymax > -delta) && ((fmax(fabs(Ymin), fabs(Ymax)) < delta) || (fabs(Ymin / Ymax) >= 1. / 2)))
+        return false;
+    return true;
+}

@@ -1,0 +1,249 @@
+"""Python host side of the GB300 GP-MOOD step: a ctypes binding of libgpmood.so.
+
+Mirrors the reference's Fortran interface for the per-step path under the
+same names: ``time_stepping`` (gp-mood-code/time_stepper.f90:12),
+``Setdt`` (gp-mood-code/physics.f90:78), ``Boundary_C`` (gp-mood-code/BC.f90:10)
+and the knobs of ``parameters.f90``.  State arrays use the reference layout
+U(4, lb:le, nb:ne), i.e. a C array of shape (nf+8, lf+8, 4).
+
+There is no CPU fallback: importing this module without the built CUDA library
+raises, and creating a Solver without a GPU raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from dataclasses import dataclass
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB_PATH = HERE / "libgpmood.so"
+
+NGC = 4
+# gp-mood-code/constants.f90:17-34
+GP_MOOD, GP_SE, NN_GP_MOOD = 2, 202, 203
+SSP_RK3 = 10
+HLLC = 100
+NEUMANN, PERIODIC, REFLECTIVE, DMR = 17, 18, 20, 35
+FP_EXACT, FP_FAST = 0, 1
+
+E_ARG, E_CUDA, E_MOOD_CAP, E_DT, E_STATE = -1, -2, -3, -4, -5
+NN_NPARAMS = 64 * 36 + 64 + 64 * 64 + 64 + 64 + 1
+
+
+class GpmoodError(RuntimeError):
+    def __init__(self, code: int, msg: str):
+        super().__init__(f"gpmood error {code}: {msg}")
+        self.code = code
+
+
+class Params(C.Structure):
+    """gpmood_params of include/gpmood.h (parameters.f90 knobs)."""
+    _fields_ = [("cfl", C.c_double), ("ell_o_dx", C.c_double), ("lx", C.c_double), ("ly", C.c_double),
+                ("tmax", C.c_double), ("integrator", C.c_int), ("method", C.c_int), ("mord", C.c_int),
+                ("ngp", C.c_int), ("dmp", C.c_int), ("u2", C.c_int), ("u2_tol", C.c_int), ("num_flux", C.c_int),
+                ("lf", C.c_int), ("nf", C.c_int), ("bc_type", C.c_int), ("nmax", C.c_int), ("fp_mode", C.c_int),
+                ("max_mood_iters", C.c_int), ("nsteps_with_no_nn", C.c_int)]
+
+
+class Counters(C.Structure):
+    _fields_ = [("detected_last_step", C.c_longlong), ("detected_total", C.c_longlong),
+                ("a_priori_last_step", C.c_longlong), ("mood_passes_last_step", C.c_longlong),
+                ("max_passes_stage", C.c_longlong), ("steps", C.c_longlong), ("status_flags", C.c_longlong)]
+
+
+# Every entry point of include/gpmood.h with its ctypes signature.
+_DP = C.POINTER(C.c_double)
+SIGNATURES = {
+    "gpmood_default_params": ([C.POINTER(Params)], C.c_int),
+    "gpmood_create": ([C.POINTER(Params), C.POINTER(C.c_void_p)], C.c_int),
+    "gpmood_destroy": ([C.c_void_p], None),
+    "gpmood_last_error": ([C.c_void_p, C.c_char_p, C.c_int], C.c_int),
+    "gpmood_get_weights": ([C.c_void_p, _DP, _DP, _DP], C.c_int),
+    "gpmood_gp_weights": ([C.POINTER(Params), _DP, _DP, _DP], C.c_int),
+    "gpmood_boundary_c": ([C.c_void_p, _DP, C.c_double], C.c_int),
+    "gpmood_setdt": ([C.c_void_p, _DP, C.c_double, _DP], C.c_int),
+    "gpmood_time_stepping": ([C.c_void_p, _DP, _DP, C.c_double, C.c_double], C.c_int),
+    "gpmood_set_state": ([C.c_void_p, _DP, C.c_double], C.c_int),
+    "gpmood_get_state": ([C.c_void_p, _DP, _DP, C.POINTER(C.c_int)], C.c_int),
+    "gpmood_get_orders": ([C.c_void_p, C.POINTER(C.c_byte)], C.c_int),
+    "gpmood_advance": ([C.c_void_p, C.c_int, C.POINTER(C.c_int)], C.c_int),
+    "gpmood_get_counters": ([C.c_void_p, C.POINTER(Counters)], C.c_int),
+    "gpmood_time_stepping_dev": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double], C.c_int),
+    "gpmood_set_nn": ([C.c_void_p, C.POINTER(C.c_float), C.c_int], C.c_int),
+}
+
+_lib: C.CDLL | None = None
+
+
+def load_library() -> C.CDLL:
+    """Load libgpmood.so; raise if it has not been built (no fallback)."""
+    global _lib
+    if _lib is None:
+        if not LIB_PATH.exists():
+            raise ImportError(f"{LIB_PATH} is missing: build it with __graft_entry__.build()")
+        L = C.CDLL(str(LIB_PATH))
+        for name, (args, res) in SIGNATURES.items():
+            f = getattr(L, name)
+            f.argtypes = args
+            f.restype = res
+        _lib = L
+    return _lib
+
+
+def _dp(a: np.ndarray):
+    return a.ctypes.data_as(_DP)
+
+
+def padded(lf: int, nf: int) -> np.ndarray:
+    """A zero state U(4, lb:le, nb:ne) as a C array of shape (nf+8, lf+8, 4)."""
+    return np.zeros((nf + 2 * NGC, lf + 2 * NGC, 4), dtype=np.float64)
+
+
+def default_params(**kw) -> Params:
+    p = Params()
+    load_library().gpmood_default_params(C.byref(p))
+    for k, v in kw.items():
+        if not hasattr(p, k):
+            raise TypeError(f"unknown knob {k}")
+        setattr(p, k, v)
+    return p
+
+
+def gp_weights(params: Params):
+    """GP_presim_sphere on the host (no GPU): zt[3][4][ngp][13], d2[2][5], inv_err[3]."""
+    zt = np.zeros((3, 4, params.ngp, 13))
+    d2 = np.zeros((2, 5))
+    inv = np.zeros(3)
+    L = load_library()
+    rc = L.gpmood_gp_weights(C.byref(params), _dp(zt), _dp(d2), _dp(inv))
+    if rc != 0:
+        buf = C.create_string_buffer(512)
+        L.gpmood_last_error(None, buf, 512)
+        raise GpmoodError(rc, buf.value.decode(errors="replace"))
+    return zt, d2, inv
+
+
+@dataclass
+class StepInfo:
+    detected: int
+    passes: int
+
+
+class Solver:
+    """One GP-MOOD context on the current GPU (gpmood_create .. gpmood_destroy)."""
+
+    def __init__(self, params: Params | None = None, **kw):
+        self.lib = load_library()
+        self.p = params if params is not None else default_params(**kw)
+        if params is not None:
+            for k, v in kw.items():
+                setattr(self.p, k, v)
+        h = C.c_void_p()
+        rc = self.lib.gpmood_create(C.byref(self.p), C.byref(h))
+        if rc != 0:
+            raise GpmoodError(rc, self._err(None))
+        self._h = h
+        self.lf, self.nf = self.p.lf, self.p.nf
+
+    def _err(self, h) -> str:
+        buf = C.create_string_buffer(512)
+        self.lib.gpmood_last_error(h, buf, 512)
+        return buf.value.decode(errors="replace")
+
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            raise GpmoodError(rc, self._err(self._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.gpmood_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    # -- shapes -----------------------------------------------------------
+    @property
+    def shape(self) -> tuple[int, int, int]:
+        return (self.nf + 2 * NGC, self.lf + 2 * NGC, 4)
+
+    def _state(self, U: np.ndarray, name: str) -> np.ndarray:
+        if U.shape != self.shape or U.dtype != np.float64 or not U.flags.c_contiguous:
+            raise ValueError(f"{name} must be a C-contiguous float64 array of shape {self.shape}")
+        return U
+
+    # -- reference-facing calls ----------------------------------------
+    def weights(self):
+        zt = np.zeros((3, 4, self.p.ngp, 13))
+        d2 = np.zeros((2, 5))
+        inv = np.zeros(3)
+        self._check(self.lib.gpmood_get_weights(self._h, _dp(zt), _dp(d2), _dp(inv)))
+        return zt, d2, inv
+
+    def Boundary_C(self, U: np.ndarray, t_rk: float = 0.0) -> None:
+        self._check(self.lib.gpmood_boundary_c(self._h, _dp(self._state(U, "U")), t_rk))
+
+    def Setdt(self, U: np.ndarray, dtfinal: float) -> float:
+        dt = C.c_double()
+        self._check(self.lib.gpmood_setdt(self._h, _dp(self._state(U, "U")), dtfinal, C.byref(dt)))
+        return dt.value
+
+    def time_stepping(self, Uin: np.ndarray, Uout: np.ndarray, t: float, dt: float) -> StepInfo:
+        self._check(self.lib.gpmood_time_stepping(self._h, _dp(self._state(Uin, "Uin")),
+                                                  _dp(self._state(Uout, "Uout")), t, dt))
+        c = self.counters()
+        return StepInfo(c.detected_last_step, c.mood_passes_last_step)
+
+    def time_stepping_ptr(self, uin_ptr: int, uout_ptr: int, t: float, dt: float) -> None:
+        """One step on host pointers (e.g. pinned torch tensors), same layout."""
+        self._check(self.lib.gpmood_time_stepping(self._h, C.cast(C.c_void_p(uin_ptr), _DP),
+                                                  C.cast(C.c_void_p(uout_ptr), _DP), t, dt))
+
+    def setdt_ptr(self, u_ptr: int, dtfinal: float) -> float:
+        dt = C.c_double()
+        self._check(self.lib.gpmood_setdt(self._h, C.cast(C.c_void_p(u_ptr), _DP), dtfinal, C.byref(dt)))
+        return dt.value
+
+    def time_stepping_dev(self, d_uin: int, d_uout: int, t: float, dt: float) -> None:
+        self._check(self.lib.gpmood_time_stepping_dev(self._h, C.c_void_p(d_uin), C.c_void_p(d_uout), t, dt))
+
+    # -- device-resident run ------------------------------------------------
+    def set_state(self, U: np.ndarray, t: float = 0.0) -> None:
+        self._check(self.lib.gpmood_set_state(self._h, _dp(self._state(U, "U")), t))
+
+    def get_state(self):
+        U = np.empty(self.shape)
+        t = C.c_double()
+        n = C.c_int()
+        self._check(self.lib.gpmood_get_state(self._h, _dp(U), C.byref(t), C.byref(n)))
+        return U, t.value, n.value
+
+    def advance(self, nsteps: int) -> int:
+        done = C.c_int()
+        self._check(self.lib.gpmood_advance(self._h, int(nsteps), C.byref(done)))
+        return done.value
+
+    def orders(self) -> np.ndarray:
+        o = np.zeros((self.nf, self.lf), dtype=np.int8)
+        self._check(self.lib.gpmood_get_orders(self._h, o.ctypes.data_as(C.POINTER(C.c_byte))))
+        return o
+
+    def counters(self) -> Counters:
+        c = Counters()
+        self._check(self.lib.gpmood_get_counters(self._h, C.byref(c)))
+        return c
+
+    def set_nn(self, params: np.ndarray) -> None:
+        a = np.ascontiguousarray(params, dtype=np.float32).ravel()
+        self._check(self.lib.gpmood_set_nn(self._h, a.ctypes.data_as(C.POINTER(C.c_float)), a.size))

@@ -1,0 +1,158 @@
+/*
+ * gpmood.h -- C ABI of the GB300 GP-MOOD step library (libgpmood.so).
+ *
+ * One SSP-RK3 step of GP-MOOD for the 2-D compressible Euler equations:
+ * GP-SE reconstruction (radius 2 -> 1 -> first order), HLLC face fluxes with
+ * Gauss quadrature, a-posteriori MOOD detection with its order cascade, and
+ * the CFL time step, all in FP64 on one GPU.
+ *
+ * The entry points replace the reference's Fortran subroutines one for one:
+ *   gpmood_time_stepping  <- time_stepping(Uin, Uout)   gp-mood-code/time_stepper.f90:12-23
+ *   gpmood_setdt          <- Setdt(Uin)                 gp-mood-code/physics.f90:78-129
+ *   gpmood_boundary_c     <- Boundary_C(U)              gp-mood-code/BC.f90:10-421
+ *   gpmood_create         <- GP_presim_sphere() + init_mesh()
+ *                                                       gp-mood-code/GP_init.f90:26-357,
+ *                                                       gp-mood-code/mesh_init.f90:10-20
+ *   gpmood_advance        <- the main.f90:145-203 time loop (device-resident state)
+ *   gpmood_params         <- the parameters.f90 knobs   gp-mood-code/problems/sedov_GPMOOD.f90:8-46
+ *
+ * Arrays cross the ABI in the reference's layout U(4, lb:le, nb:ne): the
+ * variable index (rho, rho*u, rho*v, E) is fastest, then x, then y, with
+ * ngc = 4 ghost layers (lb = 1-ngc, le = lf+ngc).  That is
+ * 4*(lf+8)*(nf+8) doubles.
+ *
+ * Conventions: every int-returning call returns 0 on success or a negative
+ * GPMOOD_E* code; gpmood_last_error() gives the message.  The library never
+ * keeps a host pointer after a call returns.  One context per host thread;
+ * each context owns one CUDA stream and all calls on it are synchronous at
+ * return.  There is no CPU fallback: without a usable GPU gpmood_create
+ * fails with GPMOOD_E_CUDA.
+ */
+#ifndef GPMOOD_H
+#define GPMOOD_H
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* Enumerations share the reference's values (gp-mood-code/constants.f90:17-34). */
+#define GPMOOD_GP_MOOD     2     /* method: GP-MOOD */
+#define GPMOOD_GP_SE       202   /* method: unlimited GP (MOOD off) */
+#define GPMOOD_NN_GP_MOOD  203   /* method: GP-MOOD with the MLP a-priori gate */
+#define GPMOOD_SSP_RK3     10    /* integrator */
+#define GPMOOD_HLLC        100   /* numFlux */
+#define GPMOOD_NEUMANN     17    /* BC_type */
+#define GPMOOD_PERIODIC    18
+#define GPMOOD_REFLECTIVE  20
+#define GPMOOD_DMR         35
+
+/* Floating-point modes of the kernels. */
+#define GPMOOD_FP_EXACT    0     /* reference operation order, no FMA contraction:
+                                    bit-identical to the CPU restatement */
+#define GPMOOD_FP_FAST     1     /* FMA contraction and reciprocal reuse */
+
+/* Error codes. */
+#define GPMOOD_OK           0
+#define GPMOOD_E_ARG       -1    /* invalid argument or unsupported knob */
+#define GPMOOD_E_CUDA      -2    /* CUDA runtime error (no GPU, OOM, launch failure) */
+#define GPMOOD_E_MOOD_CAP  -3    /* MOOD loop exceeded max_mood_iters in a stage */
+#define GPMOOD_E_DT        -4    /* time step not finite or not positive */
+#define GPMOOD_E_STATE     -5    /* call order violated (e.g. no state set) */
+
+/* Knobs of parameters.f90 (same names and meaning), plus GB300 run options. */
+typedef struct gpmood_params {
+    double cfl;           /* CFL                                      :8  */
+    double ell_o_dx;      /* GP length scale in cells                  :14 */
+    double lx, ly;        /* domain [0,Lx]x[0,Ly] (Lx_16, Ly_16)       :43-44 */
+    double tmax;          /* final time                                :41 */
+    int integrator;       /* must be GPMOOD_SSP_RK3                    :9  */
+    int method;           /* GPMOOD_GP_MOOD, GPMOOD_GP_SE, GPMOOD_NN_GP_MOOD */
+    int mord;             /* maximal order 1, 3 or 5                   :15 */
+    int ngp;              /* Gauss points per face, 1..5               :16 */
+    int dmp, u2, u2_tol;  /* MOOD checks (logical -> 0/1)              :18-20 */
+    int num_flux;         /* must be GPMOOD_HLLC                       :30 */
+    int lf, nf;           /* interior cells in x and y                 :37-38 */
+    int bc_type;          /* GPMOOD_NEUMANN/PERIODIC/REFLECTIVE/DMR    :45 */
+    int nmax;             /* step cap of the time loop                 :42 */
+    int fp_mode;          /* GPMOOD_FP_EXACT or GPMOOD_FP_FAST */
+    int max_mood_iters;   /* MOOD passes allowed per stage before GPMOOD_E_MOOD_CAP */
+    int nsteps_with_no_nn;/* gate off for the first steps (global_variables.f90:97) */
+} gpmood_params;
+
+/* Per-step and cumulative counters (global_variables.f90:71, main.f90:165-167). */
+typedef struct gpmood_counters {
+    long long detected_last_step;   /* count_detected_cell of the last step */
+    long long detected_total;       /* summed over all steps */
+    long long a_priori_last_step;   /* cells started at reduced order by the gate */
+    long long mood_passes_last_step;/* passes summed over the 3 stages */
+    long long max_passes_stage;     /* worst stage since create */
+    long long steps;                /* steps taken through this context */
+    long long status_flags;         /* bit 0: NaN/inadmissible state left in an
+                                       order-1 cell; bit 1: MOOD cap hit; bit 2: bad dt */
+} gpmood_counters;
+
+typedef struct gpmood_ctx gpmood_ctx;
+
+/* Fill the reference defaults: CFL 0.8, SSP-RK3, GP-MOOD, ell/dx 12, Mord 5,
+ * ngp 3, DMP/U2/U2_tol on, HLLC, 256x256 on [0,1]^2, Neumann, tmax 0.8. */
+int  gpmood_default_params(gpmood_params* p);
+
+/* Validate the knobs, run the GP weight precompute (host, binary128) and
+ * allocate the device work arrays on the current CUDA device. */
+int  gpmood_create(const gpmood_params* p, gpmood_ctx** out);
+void gpmood_destroy(gpmood_ctx* ctx);
+
+/* Last error message of ctx (or of the thread when ctx is NULL). */
+int  gpmood_last_error(const gpmood_ctx* ctx, char* buf, int len);
+
+/* The GP weights in use: zt[3][4][ngp][13] for ord 1,3,5 and faces iL,iT,iR,iB;
+ * d2[2][5] = (GP_d2x_sp, GP_d2y_sp) of ord 3; inv_err[3] = GP_init.f90:250 check. */
+int  gpmood_get_weights(const gpmood_ctx* ctx, double* zt, double* d2, double* inv_err);
+
+/* GP_presim_sphere alone (GP_init.f90:26-357): the same weights for a set of
+ * knobs, computed on the host without touching a GPU. */
+int  gpmood_gp_weights(const gpmood_params* p, double* zt, double* d2, double* inv_err);
+
+/* ---- reference-facing calls on host arrays (Fortran layout) ---- */
+
+/* Boundary_C(U): refill the ghost layers of a host array in place. */
+int  gpmood_boundary_c(gpmood_ctx* ctx, double* u_host, double t_rk);
+
+/* Setdt(U) with dtfinal = tmax - t: dt over all cells including ghosts. */
+int  gpmood_setdt(gpmood_ctx* ctx, const double* u_host, double dtfinal, double* dt_out);
+
+/* time_stepping(Uin, Uout): one SSP-RK3 step at time t with step dt.
+ * The reference refills the ghost layers of Uin in place; its caller then
+ * overwrites Uin with Uout (main.f90:162), so uin_host is left untouched here. */
+int  gpmood_time_stepping(gpmood_ctx* ctx, const double* uin_host, double* uout_host,
+                          double t, double dt);
+
+/* ---- device-resident stepping ---- */
+
+/* Upload a state (Fortran layout) and the time; resets the step counter. */
+int  gpmood_set_state(gpmood_ctx* ctx, const double* u_host, double t);
+/* Download state, time and step count (any pointer may be NULL). */
+int  gpmood_get_state(gpmood_ctx* ctx, double* u_host, double* t, int* niter);
+/* CellGPO(1:lf,1:nf) after the last stage ("ordr" of output.f90:128), x fastest. */
+int  gpmood_get_orders(gpmood_ctx* ctx, signed char* orders);
+/* The main.f90 loop: up to nsteps steps of Setdt + time_stepping + t += dt,
+ * stopping at tmax; *steps_done receives the steps taken (may be NULL). */
+int  gpmood_advance(gpmood_ctx* ctx, int nsteps, int* steps_done);
+int  gpmood_get_counters(const gpmood_ctx* ctx, gpmood_counters* out);
+
+/* One step on device arrays (padded layout) on the context's stream; d_uin is
+ * inout (its ghosts are refilled, as in the reference).  For callers that keep
+ * the state on the GPU. */
+int  gpmood_time_stepping_dev(gpmood_ctx* ctx, double* d_uin, double* d_uout,
+                              double t, double dt);
+
+/* ---- a-priori MLP gate (method GPMOOD_NN_GP_MOOD) ---- */
+
+/* Load the 36-64-64-1 gate: w0[64][36], b0[64], w1[64][64], b1[64], w2[64], b2[1]
+ * as one float array of 6641 values in that order (PyTorch flatten order). */
+int  gpmood_set_nn(gpmood_ctx* ctx, const float* params, int n);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,155 @@
+"""Parity of the CUDA path against the CPU oracle, through the C ABI.
+
+FP_EXACT: bit-identical states, time steps and MOOD order masks.
+FP_FAST : per-field relative L1 <= 1e-12 and identical MOOD order masks after
+          10 steps (the tolerance of the design target)."""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import nan_equal
+
+pytestmark = pytest.mark.gpu
+
+CASES = {
+    # name: (ic, lf, nf, knobs)
+    "rp2d3": ("rp2d3", 64, 64, dict(bc=17, tmax=0.8)),
+    "sedov": ("sedov", 64, 64, dict(bc=20, tmax=0.05)),
+    "dmr": ("dmr", 96, 24, dict(bc=35, lx=4.0, ly=1.0, tmax=0.2)),
+    "vortex": ("vortex", 48, 48, dict(bc=18, lx=10.0, ly=10.0, tmax=1.0)),
+    "rp2d3_r1": ("rp2d3", 64, 64, dict(bc=17, tmax=0.8, mord=3, ngp=2)),
+}
+
+
+def _solver(pkg, lf, nf, fp_mode, kn):
+    kw = dict(lf=lf, nf=nf, fp_mode=fp_mode, tmax=kn.get("tmax", 0.8), bc_type=kn.get("bc", 17),
+              lx=kn.get("lx", 1.0), ly=kn.get("ly", 1.0), mord=kn.get("mord", 5), ngp=kn.get("ngp", 3))
+    for k in ("method", "dmp", "u2", "u2_tol", "max_mood_iters"):
+        if k in kn:
+            kw[k] = kn[k]
+    return pkg.Solver(**kw)
+
+
+def _oracle_params(oracle, lf, nf, kn):
+    kw = dict(kn)
+    bc = kw.pop("bc", 17)
+    kw.pop("max_mood_iters", None)
+    return oracle.make_params(lf, nf, bc=bc, **kw)
+
+
+def _run_pair(pkg, oracle, case, nsteps, fp_mode):
+    ic, lf, nf, kn = CASES[case]
+    p = _oracle_params(oracle, lf, nf, kn)
+    U = oracle.initial_condition(p, ic)
+    st = oracle.Stepper(p)
+    Ug = U.copy()
+    t = 0.0
+    with _solver(pkg, lf, nf, fp_mode, kn) as s:
+        for step in range(nsteps):
+            dt = oracle.setdt(p, U, p.tmax - t)
+            dtg = s.Setdt(Ug, p.tmax - t)
+            Ur = np.empty_like(U)
+            masks = st.time_stepping(U, Ur, t, dt, want_orders=True)
+            Ugr = np.empty_like(Ug)
+            s.time_stepping(Ug, Ugr, t, dtg)
+            yield step, (U, Ur, dt, masks[2]), (Ugr, dtg, s.orders(), s.counters()), st
+            t += dt
+            U, Ug = Ur, Ugr
+
+
+@pytest.mark.parametrize("case", list(CASES))
+def test_exact_mode_bitwise(pkg, oracle, case):
+    nsteps = 10 if case != "dmr" else 6
+    for step, (U, Ur, dt, mask), (Ugr, dtg, mask_g, ctr), st in _run_pair(pkg, oracle, case, nsteps, pkg.FP_EXACT):
+        assert dtg == dt, (step, dtg, dt)
+        assert np.array_equal(mask_g, mask), f"order mask differs at step {step}"
+        assert nan_equal(Ugr, Ur), f"state differs at step {step}: max |d| = {np.nanmax(np.abs(Ugr - Ur))}"
+
+
+@pytest.mark.parametrize("case", ["rp2d3", "sedov", "vortex", "dmr"])
+def test_fast_mode_tolerance(pkg, oracle, case):
+    ic, lf, nf, kn = CASES[case]
+    p = _oracle_params(oracle, lf, nf, kn)
+    U = oracle.initial_condition(p, ic)
+    st = oracle.Stepper(p)
+    t = 0.0
+    masks = []
+    for _ in range(10):
+        dt = oracle.setdt(p, U, p.tmax - t)
+        Ur = np.empty_like(U)
+        masks.append(st.time_stepping(U, Ur, t, dt, want_orders=True)[2])
+        t += dt
+        U = Ur
+    U0 = oracle.initial_condition(p, ic)
+    with _solver(pkg, lf, nf, pkg.FP_FAST, kn) as s:
+        s.set_state(U0, 0.0)
+        assert s.advance(10) == 10
+        Ug, tg, n = s.get_state()
+        mask_g = s.orders()
+    assert n == 10
+    assert abs(tg - t) <= 1e-12 * t
+    interior = (slice(4, -4), slice(4, -4))
+    for k in range(4):
+        ref = U[interior + (k,)]
+        num = np.abs(Ug[interior + (k,)] - ref).sum()
+        den = np.abs(ref).sum()
+        assert num <= 1e-12 * den, (k, num / den)
+    assert np.array_equal(mask_g, masks[-1])
+
+
+def test_device_resident_advance_matches_oracle_run(pkg, oracle):
+    """gpmood_advance (Setdt fused into the last RK combination) == the main.f90 loop."""
+    ic, lf, nf, kn = CASES["sedov"]
+    p = _oracle_params(oracle, lf, nf, kn)
+    U = oracle.initial_condition(p, ic)
+    U0 = U.copy()
+    t, n = oracle.Stepper(p).run(U, 0.0, 12)
+    with _solver(pkg, lf, nf, pkg.FP_EXACT, kn) as s:
+        s.set_state(U0, 0.0)
+        assert s.advance(12) == 12
+        Ug, tg, ng = s.get_state()
+    assert (ng, tg) == (n, t)
+    assert nan_equal(Ug, U)
+
+
+def test_run_stops_at_tmax(pkg, oracle):
+    ic, lf, nf, kn = CASES["sedov"]
+    kn = dict(kn, tmax=2e-5)
+    p = _oracle_params(oracle, lf, nf, kn)
+    U = oracle.initial_condition(p, ic)
+    U0 = U.copy()
+    t, n = oracle.Stepper(p).run(U, 0.0, 1000)
+    with _solver(pkg, lf, nf, pkg.FP_EXACT, kn) as s:
+        s.set_state(U0, 0.0)
+        assert s.advance(1000) == n
+        Ug, tg, _ = s.get_state()
+    assert tg == t == 2e-5
+    assert nan_equal(Ug, U)
+
+
+def test_boundary_c_matches_oracle(pkg, oracle):
+    rng = np.random.default_rng(0)
+    for bc, lx, ly in ((17, 1., 1.), (18, 1., 1.), (20, 1., 1.), (35, 4., 1.)):
+        p = oracle.make_params(40, 24, bc=bc, lx=lx, ly=ly)
+        U = rng.uniform(0.5, 2.0, size=oracle.padded(40, 24).shape)
+        Ug = U.copy()
+        oracle.boundary(p, U, 0.013)
+        with pkg.Solver(lf=40, nf=24, bc_type=bc, lx=lx, ly=ly) as s:
+            s.Boundary_C(Ug, 0.013)
+        assert np.array_equal(U, Ug), bc
+
+
+def test_gp_se_mode(pkg, oracle):
+    """method GP_SE (MOOD off): unlimited R2 reconstruction, same bits."""
+    ic, lf, nf, kn = CASES["vortex"]
+    kn = dict(kn, method=202)
+    p = _oracle_params(oracle, lf, nf, kn)
+    U = oracle.initial_condition(p, ic)
+    dt = oracle.setdt(p, U, p.tmax)
+    Ur = np.empty_like(U)
+    oracle.Stepper(p).time_stepping(U.copy(), Ur, 0.0, dt)
+    with _solver(pkg, lf, nf, pkg.FP_EXACT, kn) as s:
+        Ug = np.empty_like(U)
+        s.time_stepping(U, Ug, 0.0, dt)
+    assert nan_equal(Ug, Ur)
