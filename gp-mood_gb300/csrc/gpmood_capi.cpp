@@ -38,8 +38,13 @@ struct gpmood_ctx {
     bool dt_pending;              // dSc->dtmin_bits holds Setdt of dU
     gpmood_counters ctr;
     NnGate* nn;                   // a-priori gate (method 203), or null
+    bool timing;                  // per-kernel CUDA-event timing
+    cudaEvent_t ev[4];
+    gpmood_timing tm;
     char err[512];
 };
+
+double gpm_probe_fp64();
 
 namespace {
 
@@ -91,19 +96,36 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* pa
     cudaStream_t s = c->stream;
     const KernelTable& kt = *c->kt;
     c->kt->bc(c->g, uin, c->dSc, stage, s);  // Boundary_C(Uin), :64
+    c->ctr.kernel_launches += 2;
     bool uniform = true;
     CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, s));  // CellGPO = mord, :48
     if (c->p.method == GPMOOD_NN_GP_MOOD && c->nn && c->niter + 1 > c->p.nsteps_with_no_nn) {
         int rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, s);  // :51-56
-        if (rc) return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
+        if (rc < 0) return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
+        c->ctr.kernel_launches += rc;
         uniform = false;
     }
     CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), s));
     StageArgs a = stage_args(c, uin, uout, stage, uniform);
+    if (c->timing) cudaEventRecord(c->ev[0], s);
     kt.flux_all(a, c->w, s);
+    if (c->timing) cudaEventRecord(c->ev[1], s);
     kt.update_detect(a, c->w, 0, s);
+    if (c->timing) cudaEventRecord(c->ev[2], s);
+    c->ctr.kernel_launches += 3;
     int rc = check_launch(c, "first MOOD pass");
     if (rc) return rc;
+    if (c->timing) {
+        float ms0 = 0.f, ms1 = 0.f;
+        cudaEventSynchronize(c->ev[2]);
+        cudaEventElapsedTime(&ms0, c->ev[0], c->ev[1]);
+        cudaEventElapsedTime(&ms1, c->ev[1], c->ev[2]);
+        c->tm.flux_ms += ms0;
+        c->tm.flux_launches += 2;
+        c->tm.flux_faces += (long long)(c->p.lf + 1) * c->p.nf + (long long)c->p.lf * (c->p.nf + 1);
+        c->tm.update_ms += ms1;
+        c->tm.update_launches += 1;
+    }
     long long npass = 1;
     if (c->p.method == GPMOOD_GP_MOOD || c->p.method == GPMOOD_NN_GP_MOOD) {
         int cur = 0;
@@ -118,15 +140,26 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* pa
                             c->p.max_mood_iters, nt);
             }
             npass++;
+            if (c->timing) cudaEventRecord(c->ev[0], s);
             kt.mood_mark(a, cur, nt, s);
             kt.mood_faces(a, c->w, cur, nt, s);
             kt.mood_cells(a, c->w, cur, nt, ++c->pass_id, s);
+            if (c->timing) cudaEventRecord(c->ev[3], s);
+            c->ctr.kernel_launches += 3;
             rc = check_launch(c, "MOOD pass");
             if (rc) return rc;
+            if (c->timing) {
+                float ms = 0.f;
+                cudaEventSynchronize(c->ev[3]);
+                cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]);
+                c->tm.mood_ms += ms;
+                c->tm.mood_faces += 4LL * nt;
+            }
             cur ^= 1;
         }
     }
     kt.bc(c->g, uout, c->dSc, stage, s);  // the last DETECTION's Boundary_C(Uout)
+    c->ctr.kernel_launches += 2;
     *passes += npass;
     if (npass > c->ctr.max_passes_stage) c->ctr.max_passes_stage = npass;
     return check_launch(c, "stage");
@@ -143,6 +176,7 @@ int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
     rc = run_stage(c, c->dU1, c->dU2, 1, &passes);
     if (rc) return rc;
     c->kt->combine(c->g, u, c->dU2, 0.75, 0.25, 0, c->dSc, s);  // U2 = 0.75 Uin + 0.25 U2
+    c->ctr.kernel_launches += 2;
     rc = run_stage(c, c->dU2, ur, 2, &passes);
     if (rc) return rc;
     c->kt->combine(c->g, u, ur, 1. / 3, 2. / 3, with_cfl ? 1 : 0, c->dSc, s);  // Uout = Uin/3 + 2 Uout/3
@@ -194,6 +228,8 @@ void free_all(gpmood_ctx* c) {
     if (c->hSc) cudaFreeHost(c->hSc);
     if (c->hCount) cudaFreeHost(c->hCount);
     if (c->nn) nn_gate_destroy(c->nn);
+    for (int i = 0; i < 4; i++)
+        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -289,6 +325,14 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
         free_all(c);
         delete c;
         return GPMOOD_E_CUDA;
+    }
+    for (int i = 0; i < 4; i++) {
+        if (cudaEventCreate(&c->ev[i]) != cudaSuccess) {
+            fail(c, GPMOOD_E_CUDA, "event creation failed");
+            free_all(c);
+            delete c;
+            return GPMOOD_E_CUDA;
+        }
     }
     memset(c->hSc, 0, sizeof(DevScalars));
     c->hSc->tmax = p->tmax;
@@ -389,6 +433,7 @@ int gpmood_setdt(gpmood_ctx* c, const double* u_host, double dtfinal, double* dt
     CU(cudaMemcpyAsync(c->dU2, u_host, state_bytes(c), cudaMemcpyHostToDevice, c->stream));
     c->kt->cfl(c->g, c->dU2, c->dSc, c->stream);
     c->kt->dt_finalize(c->g, c->dSc, dtfinal < 0.0 ? 0.0 : dtfinal, c->stream);
+    c->ctr.kernel_launches += 2;
     int rc = check_launch(c, "Setdt");
     if (rc) return rc;
     CU(cudaMemcpyAsync(c->hSc, c->dSc, sizeof(DevScalars), cudaMemcpyDeviceToHost, c->stream));
@@ -463,12 +508,15 @@ int gpmood_advance(gpmood_ctx* c, int nsteps, int* steps_done) {
     while (done < nsteps && c->t < c->p.tmax && c->niter < c->p.nmax) {  // main.f90:145
         if (!c->dt_pending) {  // Setdt(U) (main.f90:151); later steps fuse it into the last combine
             c->kt->cfl(c->g, c->dU, c->dSc, c->stream);
+            c->ctr.kernel_launches += 1;
         }
         c->kt->dt_finalize(c->g, c->dSc, -1.0, c->stream);
+        c->ctr.kernel_launches += 1;
         int rc = run_step(c, c->dU, c->dUr, true);
         if (rc) return rc;
         if (c->hSc->status & GPM_STATUS_DT) return fail(c, GPMOOD_E_DT, "Setdt produced dt = %g", c->hSc->dt);
         c->kt->advance_t(c->dSc, c->stream);  // t = t + dt
+        c->ctr.kernel_launches += 1;
         double* tmp = c->dU;                   // U = Ur
         c->dU = c->dUr;
         c->dUr = tmp;
@@ -485,6 +533,29 @@ int gpmood_advance(gpmood_ctx* c, int nsteps, int* steps_done) {
 int gpmood_get_counters(const gpmood_ctx* c, gpmood_counters* out) {
     if (!c || !out) return fail(nullptr, GPMOOD_E_ARG, "NULL argument");
     *out = c->ctr;
+    return 0;
+}
+
+void* gpmood_get_stream(const gpmood_ctx* c) { return c ? (void*)c->stream : nullptr; }
+
+int gpmood_set_timing(gpmood_ctx* c, int on) {
+    if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
+    c->timing = on != 0;
+    memset(&c->tm, 0, sizeof(c->tm));
+    return 0;
+}
+
+int gpmood_get_timing(const gpmood_ctx* c, gpmood_timing* out) {
+    if (!c || !out) return fail(nullptr, GPMOOD_E_ARG, "NULL argument");
+    *out = c->tm;
+    return 0;
+}
+
+int gpmood_probe_fp64(double* gflops) {
+    if (!gflops) return fail(nullptr, GPMOOD_E_ARG, "NULL argument");
+    const double g = gpm_probe_fp64();
+    if (!(g > 0)) return fail(nullptr, GPMOOD_E_CUDA, "FP64 probe failed: %s", cudaGetErrorString(cudaGetLastError()));
+    *gflops = g;
     return 0;
 }
 

@@ -50,7 +50,14 @@ class Params(C.Structure):
 class Counters(C.Structure):
     _fields_ = [("detected_last_step", C.c_longlong), ("detected_total", C.c_longlong),
                 ("a_priori_last_step", C.c_longlong), ("mood_passes_last_step", C.c_longlong),
-                ("max_passes_stage", C.c_longlong), ("steps", C.c_longlong), ("status_flags", C.c_longlong)]
+                ("max_passes_stage", C.c_longlong), ("steps", C.c_longlong), ("status_flags", C.c_longlong),
+                ("kernel_launches", C.c_longlong)]
+
+
+class Timing(C.Structure):
+    _fields_ = [("flux_ms", C.c_double), ("flux_launches", C.c_longlong), ("flux_faces", C.c_longlong),
+                ("update_ms", C.c_double), ("update_launches", C.c_longlong), ("mood_ms", C.c_double),
+                ("mood_faces", C.c_longlong)]
 
 
 # Every entry point of include/gpmood.h with its ctypes signature.
@@ -72,6 +79,10 @@ SIGNATURES = {
     "gpmood_get_counters": ([C.c_void_p, C.POINTER(Counters)], C.c_int),
     "gpmood_time_stepping_dev": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double], C.c_int),
     "gpmood_set_nn": ([C.c_void_p, C.POINTER(C.c_float), C.c_int], C.c_int),
+    "gpmood_get_stream": ([C.c_void_p], C.c_void_p),
+    "gpmood_set_timing": ([C.c_void_p, C.c_int], C.c_int),
+    "gpmood_get_timing": ([C.c_void_p, C.POINTER(Timing)], C.c_int),
+    "gpmood_probe_fp64": ([_DP], C.c_int),
 }
 
 _lib: C.CDLL | None = None
@@ -123,6 +134,18 @@ def gp_weights(params: Params):
         L.gpmood_last_error(None, buf, 512)
         raise GpmoodError(rc, buf.value.decode(errors="replace"))
     return zt, d2, inv
+
+
+def probe_fp64() -> float:
+    """FP64 FMA throughput of the current GPU in GFLOP/s (2 flops per FMA)."""
+    g = C.c_double()
+    L = load_library()
+    rc = L.gpmood_probe_fp64(C.byref(g))
+    if rc != 0:
+        buf = C.create_string_buffer(512)
+        L.gpmood_last_error(None, buf, 512)
+        raise GpmoodError(rc, buf.value.decode(errors="replace"))
+    return g.value
 
 
 @dataclass
@@ -243,6 +266,20 @@ class Solver:
         c = Counters()
         self._check(self.lib.gpmood_get_counters(self._h, C.byref(c)))
         return c
+
+    # -- measurement --------------------------------------------------------
+    @property
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        return int(self.lib.gpmood_get_stream(self._h) or 0)
+
+    def set_timing(self, on: bool) -> None:
+        self._check(self.lib.gpmood_set_timing(self._h, 1 if on else 0))
+
+    def timing(self) -> Timing:
+        t = Timing()
+        self._check(self.lib.gpmood_get_timing(self._h, C.byref(t)))
+        return t
 
     def set_nn(self, params: np.ndarray) -> None:
         a = np.ascontiguousarray(params, dtype=np.float32).ravel()

@@ -89,7 +89,19 @@ typedef struct gpmood_counters {
     long long steps;                /* steps taken through this context */
     long long status_flags;         /* bit 0: NaN/inadmissible state left in an
                                        order-1 cell; bit 1: MOOD cap hit; bit 2: bad dt */
+    long long kernel_launches;      /* kernels launched through this context */
 } gpmood_counters;
+
+/* Per-kernel device time gathered with CUDA events when timing is on. */
+typedef struct gpmood_timing {
+    double flux_ms;          /* first-pass face kernels (GP recon + HLLC), all launches */
+    long long flux_launches;
+    long long flux_faces;    /* faces computed by those launches */
+    double update_ms;        /* flux-difference update + DETECTION kernels */
+    long long update_launches;
+    double mood_ms;          /* MOOD passes 2, 3, ... (mark + faces + cells) */
+    long long mood_faces;    /* faces recomputed in those passes */
+} gpmood_timing;
 
 typedef struct gpmood_ctx gpmood_ctx;
 
@@ -145,6 +157,17 @@ int  gpmood_get_counters(const gpmood_ctx* ctx, gpmood_counters* out);
  * the state on the GPU. */
 int  gpmood_time_stepping_dev(gpmood_ctx* ctx, double* d_uin, double* d_uout,
                               double t, double dt);
+
+/* ---- measurement ---- */
+
+/* The context's cudaStream_t (as void*), for callers that time on it. */
+void* gpmood_get_stream(const gpmood_ctx* ctx);
+/* Turn per-kernel CUDA-event timing on (1) or off (0); on also clears it. */
+int  gpmood_set_timing(gpmood_ctx* ctx, int on);
+int  gpmood_get_timing(const gpmood_ctx* ctx, gpmood_timing* out);
+/* FP64 FMA throughput of the current GPU in GFLOP/s (2 flops per FMA),
+ * from a short dependent-chain microbenchmark; the FP64 roofline denominator. */
+int  gpmood_probe_fp64(double* gflops);
 
 /* ---- a-priori MLP gate (method GPMOOD_NN_GP_MOOD) ---- */
 
