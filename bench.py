@@ -1,0 +1,333 @@
+#!/usr/bin/env python
+"""Benchmark: FP64 cell-updates/s of the GP-MOOD step on the 2048x2048 Sedov
+point blast (plain GP-MOOD, R2 -> R1 -> first order, HLLC, SSP-RK3, CFL 0.8,
+reflecting BCs) on one GB300 per rank.
+
+A step is one pass of the hot path over the grid: Setdt + time_stepping
+(three RK stages with their MOOD loops) + t += dt.  Cell-updates/s counts
+lf*nf per step, the reference's own definition (gp-mood-code/main.f90:214-215).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+One JSON line is printed by rank 0.  --impl reference times the reference
+algorithm on the host cores instead (the CPU oracle, since the Fortran
+reference cannot be compiled on these machines).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+N_DEFAULT = 2048
+TMAX = 0.05
+# Algorithmic FP64 flops per face of the first-pass face kernel at ngp = 3,
+# counting +,-,*,/,sqrt as one flop each: two 13-point GP reconstructions of 4
+# variables at 3 Gauss points (2*3*4*25 = 600), 3 HLLC solves (3*103 = 309)
+# and the quadrature (4*5 = 20).
+FLOPS_PER_FACE = 929
+# Algorithmic HBM bytes per cell-update of one full SSP-RK3 step: each stage
+# reads its input (32 B) and writes its output (32 B); stages 2-3 also read U^n.
+BYTES_PER_CELL_UPDATE = 256
+FLOPS_PER_CELL_UPDATE = 5900
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--n", type=int, default=N_DEFAULT)
+    ap.add_argument("--fp-mode", choices=("fast", "exact"), default="fast")
+    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if (args.impl == "ours" and torch.cuda.is_available()) else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+    return ws, rank, local
+
+
+def workload_name(n):
+    return (f"2D Sedov point blast {n}x{n} on [0,1]^2, E0=1 within 3.5dx, rho=1, p=1e-5, reflecting BCs; "
+            f"plain GP-MOOD Mord=5 (R2->R1->1), ngp=3, ell=12dx, HLLC, SSP-RK3, CFL 0.8")
+
+
+class ClockSampler:
+    """nvidia-smi SM clocks and throttle reasons sampled every 200 ms."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=2)
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx.append(float(parts[1]))
+            except ValueError:
+                continue
+            for name, v in zip(names, parts[4:8]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    try:
+        return json.loads((ROOT / "MEASURED_PEAKS.json").read_text())
+    except (OSError, ValueError):
+        return None
+
+
+def ncu_traffic_per_face():
+    """DRAM bytes per face of the first-pass face kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "ncu_flux_tile_sedov.md"
+    try:
+        m = re.search(r"dram_bytes_per_face:\s*([0-9.eE+-]+)", f.read_text())
+        return float(m.group(1)) if m else None
+    except OSError:
+        return None
+
+
+def cpu_oracle_rate(n, steps, threads):
+    """Reference algorithm (the CPU oracle) on the same Sedov workload."""
+    import __graft_entry__ as ge
+    O = ge.import_oracle()
+    O.build()
+    O.set_threads(threads)
+    p = O.make_params(n, n, bc=O.REFLECTIVE, tmax=TMAX)
+    U = O.initial_condition(p, "sedov")
+    st = O.Stepper(p)
+    t0 = time.perf_counter()
+    _, k = st.run(U, 0.0, steps)
+    el = time.perf_counter() - t0
+    return n * n * k / el, k, el
+
+
+def run_reference(args, ws, rank):
+    if rank != 0:
+        return 0
+    threads = os.cpu_count() or 1
+    n = args.n
+    # Warm-up steps and timed steps of the oracle, each a full SSP-RK3 step of
+    # the same grid (bounded: the oracle takes ~1 s per 2048^2 step on 16 cores).
+    rate_w, _, _ = cpu_oracle_rate(n, max(1, min(args.warmup, 1)), threads)
+    rate, k, el = cpu_oracle_rate(n, args.steps, threads)
+    line = {
+        "impl": "reference", "metric": "FP64 cell-updates/s", "value": rate, "unit": "cell-updates/s",
+        "n_gpus": ws, "steps": k, "warmup": args.warmup, "ms_per_step": 1e3 * el / max(k, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(n), "implementation": "CPU restatement of the reference Fortran "
+                   "(oracle/gpmood_oracle.c, OpenMP); the Fortran itself has no compiler on this host"},
+        "cpu_baseline": {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+                         "sample": f"{k} SSP-RK3 steps of the {n}x{n} Sedov IC from t=0"},
+        "e2e": {"value": rate, "unit": "cell-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_ours(args, ws, rank, local):
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+
+    pkg = ge.import_package()
+    from gpmood_gb300 import ic
+    from gpmood_gb300.gpmood import probe_fp64
+
+    torch.cuda.set_device(local)
+    n, K, W = args.n, args.steps, max(args.warmup, 3)
+    fp = pkg.FP_FAST if args.fp_mode == "fast" else pkg.FP_EXACT
+    U0 = ic.sedov(n, n)
+    solver = pkg.Solver(lf=n, nf=n, bc_type=pkg.REFLECTIVE, tmax=TMAX, fp_mode=fp)
+    solver.Boundary_C(U0, 0.0)
+    state_bytes = U0.nbytes
+    peak_fp64_gflops = probe_fp64()
+
+    def barrier():
+        if ws > 1:
+            import torch.distributed as dist
+            dist.barrier()
+
+    def max_over_ranks(x: float) -> float:
+        if ws == 1:
+            return x
+        import torch.distributed as dist
+        t = torch.tensor([x], dtype=torch.float64, device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        return float(t.item())
+
+    # ---- device-resident throughput (inputs in HBM) ----
+    solver.set_state(U0, 0.0)
+    solver.advance(W)
+    stream = torch.cuda.ExternalStream(solver.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    launches0 = solver.counters().kernel_launches
+    solver.set_timing(True)
+    clocks = ClockSampler(local)
+    clocks.start()
+    barrier()
+    torch.cuda.synchronize()
+    ev0.record(stream)
+    done = solver.advance(K)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    barrier()
+    clk = clocks.stop()
+    el_ms = max_over_ranks(ev0.elapsed_time(ev1))
+    tm = solver.timing()
+    ctr = solver.counters()
+    launches = ctr.kernel_launches - launches0
+    value = ws * n * n * done / (el_ms * 1e-3)
+
+    # ---- end to end through the reference-facing C ABI with host buffers ----
+    Uh = torch.empty(U0.shape, dtype=torch.float64).pin_memory()
+    Urh = torch.empty(U0.shape, dtype=torch.float64).pin_memory()
+    Uh.numpy()[...] = U0
+    t = 0.0
+    ke = max(1, args.e2e_steps)
+    for _ in range(2):  # warm-up
+        dt = solver.setdt_ptr(Uh.data_ptr(), TMAX - t)
+        solver.time_stepping_ptr(Uh.data_ptr(), Urh.data_ptr(), t, dt)
+        t += dt
+        Uh, Urh = Urh, Uh
+    barrier()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        dt = solver.setdt_ptr(Uh.data_ptr(), TMAX - t)
+        solver.time_stepping_ptr(Uh.data_ptr(), Urh.data_ptr(), t, dt)
+        t += dt
+        Uh, Urh = Urh, Uh
+    torch.cuda.synchronize()
+    barrier()
+    e2e_s = max_over_ranks(time.perf_counter() - t0)
+    e2e = {"value": ws * n * n * ke / e2e_s, "unit": "cell-updates/s",
+           "h2d_bytes_per_step": 2 * state_bytes, "d2h_bytes_per_step": state_bytes,
+           "path": "gpmood_setdt + gpmood_time_stepping on pinned host arrays (Fortran layout)"}
+    solver.close()
+
+    # ---- roofline of the dominant kernel (first-pass face kernel) ----
+    launch_ms = tm.flux_ms / max(tm.flux_launches, 1)
+    faces_per_launch = tm.flux_faces / max(tm.flux_launches, 1)
+    achieved_tflops = FLOPS_PER_FACE * faces_per_launch / (launch_ms * 1e-3) / 1e12
+    peak_tflops = peak_fp64_gflops / 1e3
+    tpf = ncu_traffic_per_face()
+    roofline = {"bound": "fp64", "kernel": "k_flux_tile (GP recon + HLLC + quadrature)",
+                "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
+                "frac": achieved_tflops / peak_tflops,
+                "traffic": (tpf * faces_per_launch) if tpf else None,
+                "peak_source": "FP64 FMA microbenchmark (gpmood_probe_fp64) run live on this GPU; "
+                               "MEASURED_PEAKS.json has no FP64 figure",
+                "flops_per_face": FLOPS_PER_FACE, "faces_per_launch": faces_per_launch,
+                "launch_ms": launch_ms, "share_of_step": tm.flux_ms / el_ms if el_ms else None}
+    peaks = measured_peaks()
+    hbm_peak = peaks.get("hbm_gbs") if peaks else 6800.0
+    step_gbs = BYTES_PER_CELL_UPDATE * value / ws / 1e9
+    roofline_hbm = {"bound": "hbm", "achieved": step_gbs, "peak": hbm_peak, "unit": "GB/s",
+                    "frac": step_gbs / hbm_peak, "traffic": None,
+                    "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
+                    "note": "whole step, 256 algorithmic bytes per cell-update; the path is FP64-pipe bound"}
+
+    cpu = None
+    if rank == 0 and ws == 1 and args.cpu_steps > 0:
+        threads = os.cpu_count() or 1
+        rate, k, el = cpu_oracle_rate(n, args.cpu_steps, threads)
+        cpu = {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
+               "sample": f"{k} SSP-RK3 steps of the {n}x{n} Sedov IC from t=0 (CPU oracle, OpenMP)"}
+
+    line = {
+        "metric": "FP64 cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": done,
+        "warmup": W, "ms_per_step": el_ms / max(done, 1), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": workload_name(n), "variant": "plain GP-MOOD", "fp_mode": args.fp_mode,
+                   "l2": "inputs larger than L2 (each state array is %.0f MB)" % (state_bytes / 1e6),
+                   "parallelism": "replicas" if ws > 1 else "1 GPU",
+                   "mood_passes_last_step": ctr.mood_passes_last_step,
+                   "detected_last_step": ctr.detected_last_step},
+        "roofline": roofline, "roofline_hbm": roofline_hbm, "cpu_baseline": cpu, "e2e": e2e,
+        "gpu_launches": launches, "clocks": clk,
+        "fp64_peak_gflops": peak_fp64_gflops,
+        "flops_per_cell_update": FLOPS_PER_CELL_UPDATE,
+        "achieved_step_tflops": FLOPS_PER_CELL_UPDATE * value / ws / 1e12,
+    }
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup(args)
+    if args.impl == "reference":
+        rc = run_reference(args, ws, rank)
+    else:
+        rc = run_ours(args, ws, rank, local)
+    if ws > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return rc
+
+
+if __name__ == "__main__":
+    sys.exit(main())
