@@ -129,6 +129,8 @@ void gauss_rule(int ngp, f128* pt, double* w) {
 
 }  // namespace
 
+double gpm_cell_size(double length, int n) { return (double)((_Float128)length / n); }
+
 extern "C" int gpm_gp_presim(double ell_o_dx, double lx, double ly, int lf, int nf, int mord, int ngp,
                              GpWeights* out, double inv_err[3]) {
     if (!(mord == 1 || mord == 3 || mord == 5) || ngp < 1 || ngp > GPM_MAXGP || lf < 1 || nf < 1)

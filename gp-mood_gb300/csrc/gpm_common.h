@@ -81,6 +81,12 @@ struct KernelTable {
 namespace gpm_exact { extern const KernelTable table; }
 namespace gpm_fast { extern const KernelTable table; }
 
+// Store a message in the calling thread's error buffer (gpmood_last_error(NULL, ...)).
+void gpm_set_thread_error(const char* msg);
+
+// real(L_16/n, PR): the cell size rounded once from binary128 (global_variables.f90:86-88).
+double gpm_cell_size(double length, int n);
+
 // Host GP precompute (gp_weights.cpp).  Returns 0 or -1 on bad knobs.
 extern "C" int gpm_gp_presim(double ell_o_dx, double lx, double ly, int lf, int nf, int mord, int ngp,
                              GpWeights* out, double inv_err[3]);

@@ -235,6 +235,8 @@ void free_all(gpmood_ctx* c) {
 
 }  // namespace
 
+void gpm_set_thread_error(const char* msg) { snprintf(g_err, sizeof g_err, "%s", msg); }
+
 extern "C" {
 
 int gpmood_default_params(gpmood_params* p) {

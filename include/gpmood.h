@@ -158,6 +158,21 @@ int  gpmood_get_counters(const gpmood_ctx* ctx, gpmood_counters* out);
 int  gpmood_time_stepping_dev(gpmood_ctx* ctx, double* d_uin, double* d_uout,
                               double t, double dt);
 
+/* One SSP-RK3 step that allocates no memory; it has no counterpart in the
+ * reference.  For callers that cannot let a library allocate GPU memory: a
+ * host that manages all device memory through its own pool, or a real-time
+ * loop that must not stall in cudaMalloc.  d_uin (inout: ghosts refilled) and
+ * d_uout are the caller's device arrays in the padded layout; every scratch
+ * array lives in a static device buffer of ~10 MB that every GPU loading the
+ * library holds until exit, so grids are limited to (lf+8)*(nf+8) <= 264*264
+ * (GPMOOD_E_ARG beyond that).  method GP_MOOD or GP_SE.  The first call on a
+ * device looks up that buffer's address, so make it before any stream
+ * capture.  All calls share the buffer: calls that overlap on the GPU race.
+ * stream is a cudaStream_t (NULL = legacy default stream); the call is
+ * synchronous at return.  Errors: gpmood_last_error(NULL, ...). */
+int  gpmood_time_stepping_noalloc(const gpmood_params* p, double* d_uin, double* d_uout,
+                                  double t, double dt, void* stream);
+
 /* ---- measurement ---- */
 
 /* The context's cudaStream_t (as void*), for callers that time on it. */
