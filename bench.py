@@ -237,6 +237,9 @@ def run_ours(args, ws, rank, local):
     el_ms = max_over_ranks(ev0.elapsed_time(ev1))
     tm = solver.timing()
     ctr = solver.counters()
+    Uend, t_end, _ = solver.get_state()
+    checksum = {"t": t_end, "sum_rho": float(Uend[4:-4, 4:-4, 0].sum()),
+                "sum_E": float(Uend[4:-4, 4:-4, 3].sum())}
     launches = ctr.kernel_launches - launches0
     value = ws * n * n * done / (el_ms * 1e-3)
 
@@ -304,7 +307,7 @@ def run_ours(args, ws, rank, local):
                    "l2": "inputs larger than L2 (each state array is %.0f MB)" % (state_bytes / 1e6),
                    "parallelism": "replicas" if ws > 1 else "1 GPU",
                    "mood_passes_last_step": ctr.mood_passes_last_step,
-                   "detected_last_step": ctr.detected_last_step},
+                   "detected_last_step": ctr.detected_last_step, "final_state": checksum},
         "roofline": roofline, "roofline_hbm": roofline_hbm, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": clk,
         "fp64_peak_gflops": peak_fp64_gflops,

@@ -37,7 +37,13 @@ struct gpmood_ctx {
     bool have_state;
     bool dt_pending;              // dSc->dtmin_bits holds Setdt of dU
     gpmood_counters ctr;
-    NnGate* nn;                   // a-priori gate (method 203), or null
+    NnGate* nn;                   // a-priori gate and training kernels
+    int8_t* dStageOrd;            // CellGPO at the end of each RK stage (3 x ncell)
+    float *hvX, *hvY;             // attached training-sample buffers (device), or null
+    int* hvCount;
+    int hvCap;
+    float hvKeep;
+    unsigned hvSeed;
     bool timing;                  // per-kernel CUDA-event timing
     cudaEvent_t ev[4];
     gpmood_timing tm;
@@ -99,7 +105,7 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* pa
     c->ctr.kernel_launches += 2;
     bool uniform = true;
     CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, s));  // CellGPO = mord, :48
-    if (c->p.method == GPMOOD_NN_GP_MOOD && c->nn && c->niter + 1 > c->p.nsteps_with_no_nn) {
+    if (c->p.method == GPMOOD_NN_GP_MOOD && c->niter + 1 > c->p.nsteps_with_no_nn) {
         int rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, s);  // :51-56
         if (rc < 0) return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
         c->ctr.kernel_launches += rc;
@@ -157,6 +163,13 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* pa
             }
             cur ^= 1;
         }
+    }
+    CU(cudaMemcpyAsync(c->dStageOrd + (size_t)stage * c->ncell, c->dOrder, c->ncell, cudaMemcpyDeviceToDevice, s));
+    if (stage == 0 && c->hvX) {  // training samples of stage 1 (mod_FE.f90:176-181)
+        if (nn_harvest(c->g, uin, c->dOrder, c->hvX, c->hvY, c->hvCap, c->hvCount, c->hvKeep,
+                       c->hvSeed * 2654435761u + (unsigned)c->ctr.steps, s))
+            return fail(c, GPMOOD_E_CUDA, "NN harvest: %s", cudaGetErrorString(cudaGetLastError()));
+        c->ctr.kernel_launches += 1;
     }
     kt.bc(c->g, uout, c->dSc, stage, s);  // the last DETECTION's Boundary_C(Uout)
     c->ctr.kernel_launches += 2;
@@ -224,7 +237,7 @@ void free_all(gpmood_ctx* c) {
     if (!c) return;
     cudaFree(c->dU); cudaFree(c->dUr); cudaFree(c->dU1); cudaFree(c->dU2);
     cudaFree(c->dFx); cudaFree(c->dFy); cudaFree(c->dOrder); cudaFree(c->dStamp);
-    cudaFree(c->dList[0]); cudaFree(c->dList[1]); cudaFree(c->dSc);
+    cudaFree(c->dList[0]); cudaFree(c->dList[1]); cudaFree(c->dSc); cudaFree(c->dStageOrd);
     if (c->hSc) cudaFreeHost(c->hSc);
     if (c->hCount) cudaFreeHost(c->hCount);
     if (c->nn) nn_gate_destroy(c->nn);
@@ -319,6 +332,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     ALLOC(c->dList[0], c->ncell * sizeof(int));
     ALLOC(c->dList[1], c->ncell * sizeof(int));
     ALLOC(c->dSc, sizeof(DevScalars));
+    ALLOC(c->dStageOrd, 3 * c->ncell);
 #undef ALLOC
     if (cudaMallocHost((void**)&c->hSc, sizeof(DevScalars)) != cudaSuccess ||
         cudaMallocHost((void**)&c->hCount, sizeof(int)) != cudaSuccess ||
@@ -350,14 +364,12 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
         delete c;
         return GPMOOD_E_CUDA;
     }
-    if (p->method == GPMOOD_NN_GP_MOOD) {
-        c->nn = nn_gate_create(c->g);
-        if (!c->nn) {
-            fail(c, GPMOOD_E_CUDA, "NN gate allocation failed");
-            free_all(c);
-            delete c;
-            return GPMOOD_E_CUDA;
-        }
+    c->nn = nn_gate_create(c->g);
+    if (!c->nn || cudaMemset(c->dStageOrd, p->mord, 3 * c->ncell) != cudaSuccess) {
+        fail(c, GPMOOD_E_CUDA, "NN gate allocation failed");
+        free_all(c);
+        delete c;
+        return GPMOOD_E_CUDA;
     }
     *out = c;
     return 0;
@@ -505,6 +517,8 @@ int gpmood_get_orders(gpmood_ctx* c, signed char* orders) {
 int gpmood_advance(gpmood_ctx* c, int nsteps, int* steps_done) {
     if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
     if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
+    if (c->p.method == GPMOOD_NN_GP_MOOD && !nn_gate_loaded(c->nn))
+        return fail(c, GPMOOD_E_STATE, "method NN_GP_MOOD needs the gate's parameters (gpmood_set_nn)");
     if (steps_done) *steps_done = 0;
     int done = 0;
     while (done < nsteps && c->t < c->p.tmax && c->niter < c->p.nmax) {  // main.f90:145
@@ -563,10 +577,104 @@ int gpmood_probe_fp64(double* gflops) {
 
 int gpmood_set_nn(gpmood_ctx* c, const float* params, int n) {
     if (!c || !params) return fail(c, GPMOOD_E_ARG, "NULL argument");
-    if (!c->nn) return fail(c, GPMOOD_E_STATE, "context was not created with method NN_GP_MOOD (203)");
     if (n != NN_GATE_NPARAMS) return fail(c, GPMOOD_E_ARG, "expected %d gate parameters, got %d", NN_GATE_NPARAMS, n);
     if (nn_gate_set(c->nn, params, c->stream)) return fail(c, GPMOOD_E_CUDA, "NN gate upload failed");
     CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int gpmood_set_nn_threshold(gpmood_ctx* c, float thr) {
+    if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
+    nn_gate_set_threshold(c->nn, thr);
+    return 0;
+}
+
+int gpmood_nn_predict(gpmood_ctx* c, signed char* gated, long long* n_gated) {
+    if (!c || !gated) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
+    if (!nn_gate_loaded(c->nn)) return fail(c, GPMOOD_E_STATE, "no gate parameters (gpmood_set_nn)");
+    CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, c->stream));
+    CU(cudaMemsetAsync(&c->dSc->apriori_step, 0, sizeof(unsigned long long), c->stream));
+    if (nn_gate_orders(c->nn, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, c->stream) < 0)
+        return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
+    CU(cudaMemcpy2DAsync(gated, (size_t)c->p.lf, c->dOrder + (size_t)GPM_NGC * c->g.nx + GPM_NGC, (size_t)c->g.nx,
+                         (size_t)c->p.lf, (size_t)c->p.nf, cudaMemcpyDeviceToHost, c->stream));
+    unsigned long long cnt = 0;
+    CU(cudaMemcpyAsync(&cnt, &c->dSc->apriori_step, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    const size_t nint = (size_t)c->p.lf * c->p.nf;
+    for (size_t i = 0; i < nint; i++) gated[i] = gated[i] < c->p.mord ? 1 : 0;
+    if (n_gated) *n_gated = (long long)cnt;
+    return 0;
+}
+
+int gpmood_get_stage_orders(gpmood_ctx* c, int stage, signed char* orders) {
+    if (!c || !orders) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    if (stage < 0 || stage > 2) return fail(c, GPMOOD_E_ARG, "stage must be 0, 1 or 2");
+    CU(cudaMemcpy2DAsync(orders, (size_t)c->p.lf,
+                         c->dStageOrd + (size_t)stage * c->ncell + (size_t)GPM_NGC * c->g.nx + GPM_NGC,
+                         (size_t)c->g.nx, (size_t)c->p.lf, (size_t)c->p.nf, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int gpmood_nn_features(gpmood_ctx* c, float* d_x, signed char* d_const) {
+    if (!c || !d_x) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
+    if (nn_features(c->g, c->dU, d_x, reinterpret_cast<int8_t*>(d_const), c->stream))
+        return fail(c, GPMOOD_E_CUDA, "features: %s", cudaGetErrorString(cudaGetLastError()));
+    CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int gpmood_nn_harvest(gpmood_ctx* c, float* d_x, float* d_y, int capacity, float keep_negative, unsigned seed,
+                      int* d_count) {
+    if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
+    if (!d_x) {
+        c->hvX = nullptr;
+        c->hvY = nullptr;
+        c->hvCount = nullptr;
+        return 0;
+    }
+    if (!d_y || !d_count || capacity <= 0 || !(keep_negative >= 0.f && keep_negative <= 1.f))
+        return fail(c, GPMOOD_E_ARG, "harvest needs d_y, d_count, capacity > 0 and keep_negative in [0,1]");
+    c->hvX = d_x;
+    c->hvY = d_y;
+    c->hvCount = d_count;
+    c->hvCap = capacity;
+    c->hvKeep = keep_negative;
+    c->hvSeed = seed;
+    return 0;
+}
+
+int gpmood_nn_forward(const float* d_params, const float* d_x, int n, float* d_logits, void* stream) {
+    if (!d_params || !d_x || !d_logits || n <= 0) return fail(nullptr, GPMOOD_E_ARG, "bad arguments");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (nn_forward(d_params, d_x, n, d_logits, s)) return fail(nullptr, GPMOOD_E_CUDA, "nn forward launch failed");
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(nullptr, GPMOOD_E_CUDA, "nn forward: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+int gpmood_nn_loss_grad(const float* d_params, const float* d_x, const float* d_y, int n, float pos_weight,
+                        float* d_grad, float* d_loss, void* stream) {
+    if (!d_params || !d_x || !d_y || !d_grad || !d_loss || n <= 0) return fail(nullptr, GPMOOD_E_ARG, "bad arguments");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (nn_loss_grad(d_params, d_x, d_y, n, pos_weight, d_grad, d_loss, s))
+        return fail(nullptr, GPMOOD_E_CUDA, "nn loss/grad launch failed");
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(nullptr, GPMOOD_E_CUDA, "nn loss/grad: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+int gpmood_nn_adam(float* d_params, const float* d_grad, float* d_m, float* d_v, int step, float lr, float beta1,
+                   float beta2, float eps, void* stream) {
+    if (!d_params || !d_grad || !d_m || !d_v || step < 1) return fail(nullptr, GPMOOD_E_ARG, "bad arguments");
+    cudaStream_t s = static_cast<cudaStream_t>(stream);
+    if (nn_adam(d_params, d_grad, d_m, d_v, step, lr, beta1, beta2, eps, s))
+        return fail(nullptr, GPMOOD_E_CUDA, "adam launch failed");
+    cudaError_t e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return fail(nullptr, GPMOOD_E_CUDA, "adam: %s", cudaGetErrorString(e));
     return 0;
 }
 

@@ -296,6 +296,13 @@ __global__ void __launch_bounds__(THREADS) k_train(const float* __restrict__ p, 
     warp_forward(s.f, r0, p[P_B2], f);
     // rows of this thread: r0+g (lo) and r0+g+8 (hi)
     const long long rlo = (long long)blockIdx.x * ROWS + r0 + g, rhi = rlo + 8;
+    if (fwd_only) {  // no labels, gradients or loss in this mode (yin, grad, loss_out are null)
+        if (t == 0) {
+            if (rlo < n) logits_out[rlo] = f.logit_lo;
+            if (rhi < n) logits_out[rhi] = f.logit_hi;
+        }
+        return;
+    }
     float dz[2] = {0.f, 0.f};
     float lsum = 0.f;
     const float zz[2] = {f.logit_lo, f.logit_hi};
@@ -311,13 +318,6 @@ __global__ void __launch_bounds__(THREADS) k_train(const float* __restrict__ p, 
             lsum += pos_weight * yv * spn + (1.f - yv) * sp;
             dz[h] = (pos_weight * yv * (pz - 1.f) + (1.f - yv) * pz) * inv_n;
         }
-    }
-    if (fwd_only) {
-        if (t == 0) {
-            if (rlo < n) logits_out[rlo] = f.logit_lo;
-            if (rhi < n) logits_out[rhi] = f.logit_hi;
-        }
-        return;
     }
     if (t == 0) atomicAdd(&s.loss, lsum);
     // Layer 3: grad w2, b2; dh2 = dz * w2 * relu'(a2).
@@ -502,6 +502,8 @@ int nn_gate_set(NnGate* n, const float* params, cudaStream_t s) {
 }
 
 void nn_gate_set_threshold(NnGate* n, float thr) { n->thr = thr; }
+
+bool nn_gate_loaded(const NnGate* n) { return n && n->loaded; }
 
 int nn_gate_orders(NnGate* n, const GridGeom& g, const double* uin, int8_t* order, unsigned long long* count,
                    cudaStream_t s) {

@@ -32,6 +32,7 @@ void nn_gate_destroy(NnGate* n);
 // Upload FP32 parameters and pack the BF16 weight copies used by the kernels.
 int nn_gate_set(NnGate* n, const float* params, cudaStream_t s);
 void nn_gate_set_threshold(NnGate* n, float logit_threshold);
+bool nn_gate_loaded(const NnGate* n);
 // Overwrite order[] of gated interior cells with mord-2; adds the number of
 // gated cells to *count.  Returns the number of kernels launched, or -1.
 int nn_gate_orders(NnGate* n, const GridGeom& g, const double* uin, int8_t* order, unsigned long long* count,

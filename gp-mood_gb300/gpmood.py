@@ -79,6 +79,16 @@ SIGNATURES = {
     "gpmood_get_counters": ([C.c_void_p, C.POINTER(Counters)], C.c_int),
     "gpmood_time_stepping_dev": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double], C.c_int),
     "gpmood_set_nn": ([C.c_void_p, C.POINTER(C.c_float), C.c_int], C.c_int),
+    "gpmood_set_nn_threshold": ([C.c_void_p, C.c_float], C.c_int),
+    "gpmood_nn_predict": ([C.c_void_p, C.POINTER(C.c_byte), C.POINTER(C.c_longlong)], C.c_int),
+    "gpmood_get_stage_orders": ([C.c_void_p, C.c_int, C.POINTER(C.c_byte)], C.c_int),
+    "gpmood_nn_features": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "gpmood_nn_harvest": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_uint, C.c_void_p], C.c_int),
+    "gpmood_nn_forward": ([C.c_void_p, C.c_void_p, C.c_int, C.c_void_p, C.c_void_p], C.c_int),
+    "gpmood_nn_loss_grad": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_void_p, C.c_void_p,
+                             C.c_void_p], C.c_int),
+    "gpmood_nn_adam": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_int, C.c_float, C.c_float, C.c_float,
+                        C.c_float, C.c_void_p], C.c_int),
     "gpmood_get_stream": ([C.c_void_p], C.c_void_p),
     "gpmood_set_timing": ([C.c_void_p, C.c_int], C.c_int),
     "gpmood_get_timing": ([C.c_void_p, C.POINTER(Timing)], C.c_int),
@@ -286,3 +296,27 @@ class Solver:
     def set_nn(self, params: np.ndarray) -> None:
         a = np.ascontiguousarray(params, dtype=np.float32).ravel()
         self._check(self.lib.gpmood_set_nn(self._h, a.ctypes.data_as(C.POINTER(C.c_float)), a.size))
+
+    def set_nn_threshold(self, logit_threshold: float) -> None:
+        self._check(self.lib.gpmood_set_nn_threshold(self._h, float(logit_threshold)))
+
+    def nn_predict(self):
+        """Gate decision on the device-resident state: (mask [nf, lf] int8, count)."""
+        m = np.zeros((self.nf, self.lf), dtype=np.int8)
+        n = C.c_longlong()
+        self._check(self.lib.gpmood_nn_predict(self._h, m.ctypes.data_as(C.POINTER(C.c_byte)), C.byref(n)))
+        return m, n.value
+
+    def stage_orders(self, stage: int) -> np.ndarray:
+        o = np.zeros((self.nf, self.lf), dtype=np.int8)
+        self._check(self.lib.gpmood_get_stage_orders(self._h, int(stage), o.ctypes.data_as(C.POINTER(C.c_byte))))
+        return o
+
+    def nn_features(self, d_x: int, d_const: int = 0) -> None:
+        self._check(self.lib.gpmood_nn_features(self._h, C.c_void_p(d_x), C.c_void_p(d_const or None)))
+
+    def nn_harvest(self, d_x: int, d_y: int, capacity: int, keep_negative: float, seed: int, d_count: int) -> None:
+        """Attach (d_x != 0) or detach (d_x == 0) training-sample buffers."""
+        self._check(self.lib.gpmood_nn_harvest(self._h, C.c_void_p(d_x or None), C.c_void_p(d_y or None),
+                                               int(capacity), float(keep_negative), int(seed) & 0xFFFFFFFF,
+                                               C.c_void_p(d_count or None)))

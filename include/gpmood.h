@@ -186,9 +186,43 @@ int  gpmood_probe_fp64(double* gflops);
 
 /* ---- a-priori MLP gate (method GPMOOD_NN_GP_MOOD) ---- */
 
+/* The gate replaces compute_CellGPO_with_NN (gp-mood-code/mod_NN.f90:14-58):
+ * 36 FP32 features per cell (rho, rho*u, rho*v, E on the 9-point radius-2
+ * cross, each scaled by its stencil max-abs), a 36-64-64-1 MLP with ReLU and
+ * a sigmoid output in BF16 with FP32 accumulation; a positive prediction starts
+ * the cell at order mord-2; the a-posteriori DETECTION stays on unchanged. */
+
 /* Load the 36-64-64-1 gate: w0[64][36], b0[64], w1[64][64], b1[64], w2[64], b2[1]
- * as one float array of 6641 values in that order (PyTorch flatten order). */
+ * as one float array of 6641 values in that order (PyTorch flatten order, the
+ * order of neural_network/save_NN_for_fortran.py:13-23). */
 int  gpmood_set_nn(gpmood_ctx* ctx, const float* params, int n);
+/* The gate fires when the logit exceeds this value (default 0, i.e. p > 0.5). */
+int  gpmood_set_nn_threshold(gpmood_ctx* ctx, float logit_threshold);
+/* Gate decision on the device-resident state: gated[lf*nf] = 1 where the cell
+ * would start at reduced order (x fastest); *n_gated = their number. */
+int  gpmood_nn_predict(gpmood_ctx* ctx, signed char* gated, long long* n_gated);
+/* CellGPO(1:lf,1:nf) at the end of RK stage `stage` (0, 1, 2) of the last step. */
+int  gpmood_get_stage_orders(gpmood_ctx* ctx, int stage, signed char* orders);
+/* Features of the device-resident state into device arrays d_x[lf*nf][36] and
+ * d_const[lf*nf] (1 = constant stencil, never gated). */
+int  gpmood_nn_features(gpmood_ctx* ctx, float* d_x, signed char* d_const);
+/* Collect training samples while stepping (mod_append_NN_dataset.f90:11-79):
+ * after stage 1's MOOD loop of every step, each non-constant interior cell's
+ * features go to d_x[i][36] and its label (1 if the loop lowered its order) to
+ * d_y[i]; negatives are kept with probability keep_negative; d_count is a
+ * device int holding the running count (samples past capacity are dropped).
+ * d_x = NULL detaches. */
+int  gpmood_nn_harvest(gpmood_ctx* ctx, float* d_x, float* d_y, int capacity, float keep_negative,
+                       unsigned seed, int* d_count);
+/* Training kernels on device arrays (BF16 operands, FP32 accumulation); stream
+ * is a cudaStream_t (NULL = legacy default stream); synchronous at return. */
+int  gpmood_nn_forward(const float* d_params, const float* d_x, int n, float* d_logits, void* stream);
+/* Mean weighted binary cross-entropy with logits and its gradient. */
+int  gpmood_nn_loss_grad(const float* d_params, const float* d_x, const float* d_y, int n,
+                         float pos_weight, float* d_grad, float* d_loss, void* stream);
+/* One bias-corrected Adam step (step counts from 1). */
+int  gpmood_nn_adam(float* d_params, const float* d_grad, float* d_m, float* d_v, int step,
+                    float lr, float beta1, float beta2, float eps, void* stream);
 
 #ifdef __cplusplus
 }

@@ -32,8 +32,8 @@ def bf16(a: np.ndarray) -> np.ndarray:
     return b.astype(np.uint32).view(np.float32)
 
 
-def unpack(p: np.ndarray):
-    p = np.asarray(p, dtype=np.float32)
+def unpack(p: np.ndarray, dtype=np.float32):
+    p = np.asarray(p, dtype=dtype)
     W0 = p[OFFS["W0"]:OFFS["b0"]].reshape(NH, NIN)
     b0 = p[OFFS["b0"]:OFFS["W1"]]
     W1 = p[OFFS["W1"]:OFFS["b1"]].reshape(NH, NH)
@@ -56,15 +56,21 @@ def features(U: np.ndarray, lf: int, nf: int):
     return x.astype(np.float32), cst
 
 
+def _rounder(emulate_bf16):
+    if emulate_bf16:
+        return lambda a: bf16(np.asarray(a, dtype=np.float32)).astype(np.float64)
+    return lambda a: np.asarray(a, dtype=np.float64)
+
+
 def forward(p, x, emulate_bf16=True):
-    W0, b0, W1, b1, w2, b2 = unpack(p)
-    r = bf16 if emulate_bf16 else (lambda a: np.asarray(a, dtype=np.float64))
-    x64 = r(x).astype(np.float64)
-    a1 = x64 @ r(W0).astype(np.float64).T + b0
+    W0, b0, W1, b1, w2, b2 = unpack(p, np.float32 if emulate_bf16 else np.float64)
+    r = _rounder(emulate_bf16)
+    x64 = r(x)
+    a1 = x64 @ r(W0).T + b0
     h1 = np.maximum(a1, 0)
-    a2 = r(h1.astype(np.float32)).astype(np.float64) @ r(W1).astype(np.float64).T + b1
+    a2 = r(h1) @ r(W1).T + b1
     h2 = np.maximum(a2, 0)
-    z = r(h2.astype(np.float32)).astype(np.float64) @ r(w2).astype(np.float64) + b2
+    z = r(h2) @ r(w2) + b2
     return z, (x64, a1, h1, a2, h2)
 
 
@@ -74,26 +80,26 @@ def softplus(z):
 
 def loss_grad(p, x, y, pos_weight=1.0, emulate_bf16=True):
     """Mean weighted BCE with logits and its gradient (float64)."""
-    W0, b0, W1, b1, w2, b2 = unpack(p)
-    r = bf16 if emulate_bf16 else (lambda a: np.asarray(a, dtype=np.float64))
+    W0, b0, W1, b1, w2, b2 = unpack(p, np.float32 if emulate_bf16 else np.float64)
+    r = _rounder(emulate_bf16)
     y = np.asarray(y, dtype=np.float64)
     n = len(y)
     z, (x64, a1, h1, a2, h2) = forward(p, x, emulate_bf16)
     loss = np.mean(pos_weight * y * softplus(-z) + (1 - y) * softplus(z))
     s = 1 / (1 + np.exp(-z))
     dz = (pos_weight * y * (s - 1) + (1 - y) * s) / n
-    h2b = r(h2.astype(np.float32)).astype(np.float64)
+    h2b = r(h2)
     g_w2 = dz @ h2b
     g_b2 = dz.sum()
-    w2b = r(w2).astype(np.float64)
+    w2b = r(w2)
     dh2 = np.where(a2 > 0, dz[:, None] * w2b[None, :], 0.0)
     g_b1 = dh2.sum(axis=0)
-    dh2b = r(dh2.astype(np.float32)).astype(np.float64)
-    h1b = r(h1.astype(np.float32)).astype(np.float64)
+    dh2b = r(dh2)
+    h1b = r(h1)
     g_W1 = dh2b.T @ h1b
-    dh1 = np.where(a1 > 0, dh2b @ r(W1).astype(np.float64), 0.0)
+    dh1 = np.where(a1 > 0, dh2b @ r(W1), 0.0)
     g_b0 = dh1.sum(axis=0)
-    dh1b = r(dh1.astype(np.float32)).astype(np.float64)
+    dh1b = r(dh1)
     g_W0 = dh1b.T @ x64
     g = np.concatenate([g_W0.ravel(), g_b0, g_W1.ravel(), g_b1, g_w2, [g_b2]])
     return loss, g
