@@ -8,6 +8,7 @@
 #include <math.h>
 #include <stdarg.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <new>
@@ -45,6 +46,7 @@ struct gpmood_ctx {
     float hvKeep;
     unsigned hvSeed;
     bool timing;                  // per-kernel CUDA-event timing
+    bool trace;                   // GPMOOD_TRACE=1: one line per step on stderr
     cudaEvent_t ev[4];
     gpmood_timing tm;
     char err[512];
@@ -300,6 +302,10 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     c->g.u2_tol = p->u2_tol;
     c->ncell = (size_t)c->g.nx * c->g.ny;
     c->kt = p->fp_mode == GPMOOD_FP_FAST ? &gpm_fast::table : &gpm_exact::table;
+    {
+        const char* tr = getenv("GPMOOD_TRACE");
+        c->trace = tr && tr[0] == '1';
+    }
     if (gpm_gp_presim(p->ell_o_dx, p->lx, p->ly, p->lf, p->nf, p->mord, p->ngp, &c->w, c->inv_err)) {
         delete c;
         return fail(nullptr, GPMOOD_E_ARG, "GP precompute rejected the knobs");
@@ -354,18 +360,23 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     c->hSc->tmax = p->tmax;
     c->hSc->cfl = p->cfl;
     c->hSc->dtmin_bits = 0x46293e5939a08ceaULL;  // bits of 1.0e30
-    if (cudaMemcpy(c->dSc, c->hSc, sizeof(DevScalars), cudaMemcpyHostToDevice) != cudaSuccess ||
-        cudaMemset(c->dStamp, 0, c->ncell * sizeof(unsigned)) != cudaSuccess ||
-        cudaMemset(c->dFx, 0, sb) != cudaSuccess || cudaMemset(c->dFy, 0, sb) != cudaSuccess ||
-        cudaMemset(c->dU, 0, sb) != cudaSuccess || cudaMemset(c->dUr, 0, sb) != cudaSuccess ||
-        cudaMemset(c->dU1, 0, sb) != cudaSuccess || cudaMemset(c->dU2, 0, sb) != cudaSuccess) {
+    // Initialise on the context's own stream: it is non-blocking, so work on the
+    // legacy default stream would not be ordered before its first kernels.
+    cudaStream_t s0 = c->stream;
+    if (cudaMemcpyAsync(c->dSc, c->hSc, sizeof(DevScalars), cudaMemcpyHostToDevice, s0) != cudaSuccess ||
+        cudaMemsetAsync(c->dStamp, 0, c->ncell * sizeof(unsigned), s0) != cudaSuccess ||
+        cudaMemsetAsync(c->dFx, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dFy, 0, sb, s0) != cudaSuccess ||
+        cudaMemsetAsync(c->dU, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dUr, 0, sb, s0) != cudaSuccess ||
+        cudaMemsetAsync(c->dU1, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dU2, 0, sb, s0) != cudaSuccess ||
+        cudaMemsetAsync(c->dStageOrd, p->mord, 3 * c->ncell, s0) != cudaSuccess ||
+        cudaStreamSynchronize(s0) != cudaSuccess) {
         fail(c, GPMOOD_E_CUDA, "device initialisation failed");
         free_all(c);
         delete c;
         return GPMOOD_E_CUDA;
     }
     c->nn = nn_gate_create(c->g);
-    if (!c->nn || cudaMemset(c->dStageOrd, p->mord, 3 * c->ncell) != cudaSuccess) {
+    if (!c->nn) {
         fail(c, GPMOOD_E_CUDA, "NN gate allocation failed");
         free_all(c);
         delete c;
@@ -538,6 +549,9 @@ int gpmood_advance(gpmood_ctx* c, int nsteps, int* steps_done) {
         c->dUr = tmp;
         c->t = c->hSc->t + c->hSc->dt;
         c->niter++;
+        if (c->trace)
+            fprintf(stderr, "[gpmood] step %d t=%.9e dt=%.9e detected=%lld passes=%lld status=%d\n", c->niter,
+                    c->t, c->hSc->dt, c->ctr.detected_last_step, c->ctr.mood_passes_last_step, c->hSc->status);
         c->dt_pending = true;
         done++;
         if (steps_done) *steps_done = done;

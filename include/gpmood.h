@@ -193,7 +193,7 @@ int  gpmood_probe_fp64(double* gflops);
  * the cell at order mord-2; the a-posteriori DETECTION stays on unchanged. */
 
 /* Load the 36-64-64-1 gate: w0[64][36], b0[64], w1[64][64], b1[64], w2[64], b2[1]
- * as one float array of 6641 values in that order (PyTorch flatten order, the
+ * as one float array of 6593 values in that order (PyTorch flatten order, the
  * order of neural_network/save_NN_for_fortran.py:13-23). */
 int  gpmood_set_nn(gpmood_ctx* ctx, const float* params, int n);
 /* The gate fires when the logit exceeds this value (default 0, i.e. p > 0.5). */

@@ -76,10 +76,10 @@ def test_forward_and_gradient_match_oracle(pkg, nno):
 def test_adam_step(pkg):
     from gpmood_gb300 import nn_train as T
     rng = np.random.default_rng(2)
-    p = rng.normal(size=6641).astype(np.float32)
-    g = rng.normal(size=6641).astype(np.float32)
-    m = rng.normal(size=6641).astype(np.float32) * 0.1
-    v = rng.uniform(size=6641).astype(np.float32) * 0.1
+    p = rng.normal(size=6593).astype(np.float32)
+    g = rng.normal(size=6593).astype(np.float32)
+    m = rng.normal(size=6593).astype(np.float32) * 0.1
+    v = rng.uniform(size=6593).astype(np.float32) * 0.1
     dp, dg, dm, dv = (torch.from_numpy(a.copy()).cuda() for a in (p, g, m, v))
     T.adam(dp.data_ptr(), dg.data_ptr(), dm.data_ptr(), dv.data_ptr(), 3, 1e-3)
     b1, b2, eps = 0.9, 0.999, 1e-8
@@ -88,7 +88,7 @@ def test_adam_step(pkg):
     lr_t = 1e-3 * np.sqrt(1 - b2 ** 3) / (1 - b1 ** 3)
     p1 = p - lr_t * m1 / (np.sqrt(v1) + eps)
     np.testing.assert_allclose(dp.cpu().numpy(), p1, rtol=1e-5, atol=1e-7)
-    np.testing.assert_allclose(dm.cpu().numpy(), m1, rtol=1e-6)
+    np.testing.assert_allclose(dm.cpu().numpy(), m1, rtol=1e-5, atol=1e-7)
 
 
 def test_gate_decision_matches_oracle(pkg, oracle, nno):
