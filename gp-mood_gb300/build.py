@@ -47,7 +47,7 @@ def _jobs() -> list[tuple[list[str], Path]]:
         obj = BUILD / (Path(src).stem + ".o")
         jobs.append(([nvcc, *common, "-c", str(CSRC / src), "-o", str(obj)], obj))
     gxx = shutil.which("g++") or "g++"
-    for src in ("gp_weights.cpp", "gpmood_capi.cpp"):
+    for src in ("gp_weights.cpp", "gpmood_capi.cpp", "batch_capi.cpp"):
         obj = BUILD / (Path(src).stem + ".o")
         jobs.append(([gxx, "-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-I", str(cuda / "include"),
                       "-I", str(CSRC), "-I", str(INCLUDE), "-c", str(CSRC / src), "-o", str(obj)], obj))

@@ -39,12 +39,18 @@ struct DevScalars {
     unsigned long long dtmin_bits;    // Setdt reduction slot (bits of a positive double)
     int ntrb[2];                      // troubled-cell counts, double-buffered lists
     int status;                       // GPMOOD status bits
-    int pad;
+    int passes;                       // MOOD passes of the last stage (device loop)
     unsigned long long detected_step; // count_detected_cell of the current step
     unsigned long long apriori_step;
 };
 
-enum { GPM_STATUS_NAN = 1, GPM_STATUS_MOODCAP = 2, GPM_STATUS_DT = 4 };
+enum { GPM_STATUS_NAN = 1, GPM_STATUS_MOODCAP = 2, GPM_STATUS_DT = 4, GPM_STATUS_BARRIER = 8 };
+
+// Grid barrier state of the cooperative MOOD-loop kernel (zeroed device memory).
+struct GridBar {
+    unsigned count, gen;
+    int err, pad;
+};
 
 // Launch-time arguments of one RK stage.
 struct StageArgs {
@@ -76,6 +82,9 @@ struct KernelTable {
     void (*cfl)(const GridGeom& g, const double* u, DevScalars* sc, cudaStream_t s);
     void (*dt_finalize)(const GridGeom& g, DevScalars* sc, double dtfinal, cudaStream_t s);
     void (*advance_t)(DevScalars* sc, cudaStream_t s);
+    // MOOD passes 2, 3, ... in one cooperative launch; returns -1 if the launch failed
+    int (*mood_loop)(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, unsigned pass_base,
+                     cudaStream_t s);
 };
 
 namespace gpm_exact { extern const KernelTable table; }

@@ -31,6 +31,8 @@ struct gpmood_ctx {
     int* dList[2];
     DevScalars* dSc;
     DevScalars* hSc;              // pinned mirror
+    GridBar* dBar;                // barrier of the cooperative MOOD loop
+    GridBar* hBar;                // pinned mirror
     int* hCount;                  // pinned troubled count
     unsigned pass_id;
     double t;                     // host mirror of the time
@@ -136,34 +138,30 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* pa
     }
     long long npass = 1;
     if (c->p.method == GPMOOD_GP_MOOD || c->p.method == GPMOOD_NN_GP_MOOD) {
-        int cur = 0;
-        for (;;) {
-            CU(cudaMemcpyAsync(c->hCount, &c->dSc->ntrb[cur], sizeof(int), cudaMemcpyDeviceToHost, s));
-            CU(cudaStreamSynchronize(s));
-            const int nt = *c->hCount;
-            if (nt == 0) break;  // MOOD_finished
-            if (npass >= c->p.max_mood_iters) {
-                c->ctr.status_flags |= GPM_STATUS_MOODCAP;
-                return fail(c, GPMOOD_E_MOOD_CAP, "MOOD loop did not converge in %d passes (%d troubled cells left)",
-                            c->p.max_mood_iters, nt);
-            }
-            npass++;
-            if (c->timing) cudaEventRecord(c->ev[0], s);
-            kt.mood_mark(a, cur, nt, s);
-            kt.mood_faces(a, c->w, cur, nt, s);
-            kt.mood_cells(a, c->w, cur, nt, ++c->pass_id, s);
-            if (c->timing) cudaEventRecord(c->ev[3], s);
-            c->ctr.kernel_launches += 3;
-            rc = check_launch(c, "MOOD pass");
-            if (rc) return rc;
-            if (c->timing) {
-                float ms = 0.f;
-                cudaEventSynchronize(c->ev[3]);
-                cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]);
-                c->tm.mood_ms += ms;
-                c->tm.mood_faces += 4LL * nt;
-            }
-            cur ^= 1;
+        // passes 2, 3, ... run on the device in one cooperative launch (the loop
+        // of mod_FE.f90:69-174 ends when DETECTION flags no cell)
+        const long long cap = c->p.max_mood_iters > 0 ? c->p.max_mood_iters : 2LL * c->p.lf * c->p.nf + 2;
+        const int max_pass = cap > 0x7fffffff ? 0x7fffffff : (int)cap;
+        CU(cudaMemsetAsync(c->dBar, 0, sizeof(GridBar), s));
+        if (c->timing) cudaEventRecord(c->ev[0], s);
+        if (kt.mood_loop(a, c->w, c->dBar, max_pass, c->pass_id, s))
+            return fail(c, GPMOOD_E_CUDA, "MOOD loop launch: %s", cudaGetErrorString(cudaGetLastError()));
+        if (c->timing) cudaEventRecord(c->ev[3], s);
+        c->ctr.kernel_launches += 1;
+        CU(cudaMemcpyAsync(c->hSc, c->dSc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+        CU(cudaMemcpyAsync(c->hBar, c->dBar, sizeof(GridBar), cudaMemcpyDeviceToHost, s));
+        CU(cudaStreamSynchronize(s));
+        if (c->timing) {
+            float ms = 0.f;
+            cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]);
+            c->tm.mood_ms += ms;
+        }
+        if (c->hBar->err) return fail(c, GPMOOD_E_CUDA, "MOOD loop: grid barrier timed out");
+        npass = c->hSc->passes;
+        c->pass_id += (unsigned)npass;  // stamps of later passes stay unique
+        if (c->hSc->status & GPM_STATUS_MOODCAP) {
+            c->ctr.status_flags |= GPM_STATUS_MOODCAP;
+            return fail(c, GPMOOD_E_MOOD_CAP, "MOOD loop did not converge in %d passes", max_pass);
         }
     }
     CU(cudaMemcpyAsync(c->dStageOrd + (size_t)stage * c->ncell, c->dOrder, c->ncell, cudaMemcpyDeviceToDevice, s));
@@ -231,7 +229,7 @@ int validate(const gpmood_params* p, char* why, size_t n) {
         p->bc_type != GPMOOD_DMR) { snprintf(why, n, "BC_type %d unsupported", p->bc_type); return -1; }
     if (!(p->cfl > 0) || !(p->lx > 0) || !(p->ly > 0) || !(p->ell_o_dx > 0)) { snprintf(why, n, "CFL, Lx, Ly, ell_o_dx must be > 0"); return -1; }
     if (p->fp_mode != GPMOOD_FP_EXACT && p->fp_mode != GPMOOD_FP_FAST) { snprintf(why, n, "fp_mode %d unknown", p->fp_mode); return -1; }
-    if (p->max_mood_iters < 1) { snprintf(why, n, "max_mood_iters must be >= 1"); return -1; }
+    if (p->max_mood_iters < 0) { snprintf(why, n, "max_mood_iters must be >= 0 (0: no cap but termination)"); return -1; }
     return 0;
 }
 
@@ -239,7 +237,8 @@ void free_all(gpmood_ctx* c) {
     if (!c) return;
     cudaFree(c->dU); cudaFree(c->dUr); cudaFree(c->dU1); cudaFree(c->dU2);
     cudaFree(c->dFx); cudaFree(c->dFy); cudaFree(c->dOrder); cudaFree(c->dStamp);
-    cudaFree(c->dList[0]); cudaFree(c->dList[1]); cudaFree(c->dSc); cudaFree(c->dStageOrd);
+    cudaFree(c->dList[0]); cudaFree(c->dList[1]); cudaFree(c->dSc); cudaFree(c->dStageOrd); cudaFree(c->dBar);
+    if (c->hBar) cudaFreeHost(c->hBar);
     if (c->hSc) cudaFreeHost(c->hSc);
     if (c->hCount) cudaFreeHost(c->hCount);
     if (c->nn) nn_gate_destroy(c->nn);
@@ -272,7 +271,7 @@ int gpmood_default_params(gpmood_params* p) {
     p->bc_type = GPMOOD_NEUMANN;
     p->nmax = 1 << 30;
     p->fp_mode = GPMOOD_FP_EXACT;
-    p->max_mood_iters = 64;
+    p->max_mood_iters = 0;
     p->nsteps_with_no_nn = 0;
     return 0;
 }
@@ -339,9 +338,11 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     ALLOC(c->dList[1], c->ncell * sizeof(int));
     ALLOC(c->dSc, sizeof(DevScalars));
     ALLOC(c->dStageOrd, 3 * c->ncell);
+    ALLOC(c->dBar, sizeof(GridBar));
 #undef ALLOC
     if (cudaMallocHost((void**)&c->hSc, sizeof(DevScalars)) != cudaSuccess ||
         cudaMallocHost((void**)&c->hCount, sizeof(int)) != cudaSuccess ||
+        cudaMallocHost((void**)&c->hBar, sizeof(GridBar)) != cudaSuccess ||
         cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking) != cudaSuccess) {
         fail(c, GPMOOD_E_CUDA, "pinned memory / stream creation failed");
         free_all(c);

@@ -129,7 +129,7 @@ extern "C" int gpmood_time_stepping_noalloc(const gpmood_params* p, double* d_ui
         p->ngp < 1 || p->ngp > 5 || p->lf < 4 || p->nf < 4 ||
         (p->bc_type != GPMOOD_NEUMANN && p->bc_type != GPMOOD_PERIODIC && p->bc_type != GPMOOD_REFLECTIVE &&
          p->bc_type != GPMOOD_DMR) ||
-        (p->fp_mode != GPMOOD_FP_EXACT && p->fp_mode != GPMOOD_FP_FAST) || p->max_mood_iters < 1)
+        (p->fp_mode != GPMOOD_FP_EXACT && p->fp_mode != GPMOOD_FP_FAST) || p->max_mood_iters < 0)
         return nerr(GPMOOD_E_ARG, "unsupported knobs (GP_MOOD/GP_SE, SSP-RK3, HLLC, Mord 1/3/5, ngp 1..5)");
     if (!(dt > 0) || dt != dt || dt > 1e300) return nerr(GPMOOD_E_DT, "dt must be finite and > 0");
     const size_t ncell = (size_t)(p->lf + 2 * GPM_NGC) * (size_t)(p->nf + 2 * GPM_NGC);
@@ -185,11 +185,13 @@ extern "C" int gpmood_time_stepping_noalloc(const gpmood_params* p, double* d_ui
     NCU(cudaMemcpyAsync(s.sc, &h, sizeof h, cudaMemcpyHostToDevice, st));
     NCU(cudaMemsetAsync(s.stamp, 0, ncell * sizeof(unsigned), st));  // pass ids restart at 1 every call
     unsigned pass_id = 0;
-    int rc = stage_noalloc(kt, g, w, s, d_uin, s.u1, 0, p->max_mood_iters, &pass_id, st);
-    if (!rc) rc = stage_noalloc(kt, g, w, s, s.u1, s.u2, 1, p->max_mood_iters, &pass_id, st);
+    // 0 allows 2*lf*nf+2 passes, more than a terminating MOOD loop can take
+    const int max_iters = p->max_mood_iters > 0 ? p->max_mood_iters : 2 * p->lf * p->nf + 2;
+    int rc = stage_noalloc(kt, g, w, s, d_uin, s.u1, 0, max_iters, &pass_id, st);
+    if (!rc) rc = stage_noalloc(kt, g, w, s, s.u1, s.u2, 1, max_iters, &pass_id, st);
     if (!rc) {
         kt.combine(g, d_uin, s.u2, 0.75, 0.25, 0, s.sc, st);
-        rc = stage_noalloc(kt, g, w, s, s.u2, d_uout, 2, p->max_mood_iters, &pass_id, st);
+        rc = stage_noalloc(kt, g, w, s, s.u2, d_uout, 2, max_iters, &pass_id, st);
     }
     if (!rc) {
         kt.combine(g, d_uin, d_uout, 1. / 3, 2. / 3, 0, s.sc, st);

@@ -90,7 +90,7 @@ __global__ void k_bc_x(GridGeom g, double* __restrict__ u, const DevScalars* __r
 }
 
 __global__ void k_bc_y(GridGeom g, double* __restrict__ u, const DevScalars* __restrict__ sc, int stage) {
-    const int l = -3 + blockIdx.x * blockDim.y + threadIdx.y;  // every column incl. ghosts
+    const int l = (int)(blockIdx.x * blockDim.y + threadIdx.y) - 3;  // every column incl. ghosts
     const int k = threadIdx.x;
     if (l > g.lf + GPM_NGC || k >= 2 * GPM_NGC) return;
     const bool top = k >= GPM_NGC;
@@ -370,6 +370,131 @@ __global__ void __launch_bounds__(256) k_mood_cells(StageArgs a, const __grid_co
     }
 }
 
+// ---------------------------------------------------------------------------
+// The whole MOOD loop on the device: one cooperative launch runs passes 2, 3,
+// ... until the troubled list is empty, with grid barriers between the three
+// phases of a pass (cascade, faces, crosses).  Every CTA is co-resident
+// (cooperative launch), so the barrier cannot wait on an unscheduled CTA; its
+// spin is still bounded, and a timeout records GPM_STATUS_BARRIER and makes
+// every CTA leave.
+
+__device__ __forceinline__ bool grid_sync(GridBar* b) {
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        volatile unsigned* vgen = &b->gen;
+        const unsigned g = *vgen;
+        __threadfence();
+        if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
+            atomicExch(&b->count, 0u);
+            __threadfence();
+            atomicAdd(&b->gen, 1u);
+        } else {
+            long long it = 0;
+            while (*vgen == g) {
+                if (++it > (1LL << 24)) {  // ~1 s: far beyond any pass
+                    atomicExch(&b->err, 1);
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        __threadfence();
+    }
+    __syncthreads();
+    return *(volatile int*)&b->err == 0;
+}
+
+template <int NGP>
+__global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_constant__ GpWeights w, GridBar* bar,
+                                                      int max_pass, unsigned pass_base) {
+    const GridGeom& g = a.g;
+    const double qx = a.sc->qx, qy = a.sc->qy;
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    int cur = 0, pass = 1;  // pass 1 (all faces) ran before this kernel
+    for (;;) {
+        const int nt = *(volatile int*)&a.sc->ntrb[cur];
+        if (nt == 0) break;
+        if (pass >= max_pass) {
+            if (gtid == 0) a.sc->status |= GPM_STATUS_MOODCAP;
+            break;
+        }
+        pass++;
+        // cascade of the troubled cells' orders, mod_subroutine_MOOD.f90:159-163
+        for (int i = gtid; i < nt; i += gstride) {
+            const int c = a.tlist[cur][i];
+            const int o = a.order[c];
+            a.order[c] = (int8_t)(o == 3 ? 1 : (o > 3 ? 3 : o));
+        }
+        if (gtid == 0) {
+            a.sc->ntrb[cur ^ 1] = 0;
+            a.sc->detected_step += (unsigned long long)nt;
+        }
+        if (!grid_sync(bar)) return;
+        // the four faces of every troubled cell at the new orders
+        for (int i = gtid; i < 4 * nt; i += gstride) {
+            const size_t c = (size_t)a.tlist[cur][i >> 2];
+            const int f = i & 3;
+            if ((f & 1) == 0) face_any_order<0, NGP>(a, w, f == 0 ? c - 1 : c);
+            else face_any_order<1, NGP>(a, w, f == 1 ? c - g.nx : c);
+        }
+        if (!grid_sync(bar)) return;
+        // the 5-point crosses: Uout from Uin and the current fluxes, DETECTION
+        const unsigned pid = pass_base + (unsigned)pass;
+        const int nxt = cur ^ 1, total = 5 * nt;
+        const int lim = ((total + gstride - 1) / gstride) * gstride;
+        for (int i = gtid; i < lim; i += gstride) {
+            bool trb = false;
+            int cval = 0;
+            if (i < total) {
+                const size_t t = (size_t)a.tlist[cur][i / 5];
+                const int k = i % 5;
+                const size_t c = k == 0 ? t - g.nx : k == 1 ? t - 1 : k == 2 ? t : k == 3 ? t + 1 : t + g.nx;
+                const int l = (int)(c % (size_t)g.nx) - 3, n = (int)(c / (size_t)g.nx) - 3;
+                if (l >= 1 && l <= g.lf && n >= 1 && n <= g.nf && atomicExch(&a.stamp[c], pid) != pid) {
+                    const Cell uo = cell_update(g, a.uin, a.fx, a.fy, c, qx, qy);
+                    st_cell(a.uout + 4 * c, uo);
+                    if (a.order[c] > 1) trb = mood_troubled(uo, a.uin + 4 * c, g.nx, g, w.d2x, w.d2y);
+                    cval = (int)c;
+                }
+            }
+            list_append(trb, a.tlist[nxt], &a.sc->ntrb[nxt], cval);
+        }
+        if (!grid_sync(bar)) return;
+        cur ^= 1;
+    }
+    if (gtid == 0) a.sc->passes = pass;
+}
+
+template <int NGP>
+static int launch_mood_loop_n(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, unsigned pass_base,
+                              cudaStream_t s) {
+    static int grid = 0;
+    if (!grid) {
+        int dev = 0, sms = 0, occ = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mood_loop<NGP>, 256, 0);
+        grid = sms * (occ > 0 ? occ : 1);
+    }
+    StageArgs aa = a;
+    GpWeights ww = w;
+    void* args[] = {&aa, &ww, &bar, &max_pass, &pass_base};
+    return cudaLaunchCooperativeKernel((const void*)k_mood_loop<NGP>, dim3(grid), dim3(256), args, 0, s) == cudaSuccess
+               ? 0
+               : -1;
+}
+
+int launch_mood_loop(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, unsigned pass_base,
+                     cudaStream_t s) {
+    switch (a.g.ngp) {
+    case 1: return launch_mood_loop_n<1>(a, w, bar, max_pass, pass_base, s);
+    case 2: return launch_mood_loop_n<2>(a, w, bar, max_pass, pass_base, s);
+    case 3: return launch_mood_loop_n<3>(a, w, bar, max_pass, pass_base, s);
+    case 4: return launch_mood_loop_n<4>(a, w, bar, max_pass, pass_base, s);
+    default: return launch_mood_loop_n<5>(a, w, bar, max_pass, pass_base, s);
+    }
+}
+
 static int list_grid(int max_items, int threads) {
     int dev = 0, sms = 152;
     cudaGetDevice(&dev);
@@ -488,8 +613,489 @@ void launch_dt_finalize(const GridGeom& g, DevScalars* sc, double dtfinal, cudaS
 __global__ void k_advance_t(DevScalars* sc) { sc->t = sc->t + sc->dt; }  // main.f90:160
 void launch_advance_t(DevScalars* sc, cudaStream_t s) { k_advance_t<<<1, 1, 0, s>>>(sc); }
 
-const KernelTable table = {launch_bc,        launch_flux_all,  launch_update_detect, launch_mood_mark,
-                           launch_mood_faces, launch_mood_cells, launch_combine,      launch_cfl,
-                           launch_dt_finalize, launch_advance_t};
+const KernelTable table = {launch_bc,          launch_flux_all,   launch_update_detect, launch_mood_mark,
+                           launch_mood_faces,  launch_mood_cells, launch_combine,       launch_cfl,
+                           launch_dt_finalize, launch_advance_t,  launch_mood_loop};
+
+}  // namespace GPM_NS
+
+// ===========================================================================
+// Batched stepping: many independent problems of uneven size (batch_common.h).
+// Every phase of an RK stage is one persistent launch over all problems'
+// work items, so a whole step has a fixed launch sequence that is captured
+// once as a CUDA graph.  Per-problem arithmetic is the single-problem path's.
+#include "batch_common.h"
+
+namespace GPM_NS {
+
+__device__ __forceinline__ GridGeom bgeom(const BatchArgs& a, const BProb& p) {
+    GridGeom g;
+    g.lf = p.lf; g.nf = p.nf; g.nx = p.nx; g.ny = p.ny;
+    g.dx = p.dx; g.dy = p.dy;
+    g.bc_type = a.bc_type; g.ngp = a.ngp; g.mord = a.mord; g.method = a.method;
+    g.dmp = a.dmp; g.u2 = a.u2; g.u2_tol = a.u2_tol; g.pad = 0;
+    return g;
+}
+
+// Boundary_C of every problem: blockIdx.y is the problem.
+__global__ void kb_bc_x(BatchArgs a, double* __restrict__ u) {
+    const BProb P = a.prob[blockIdx.y];
+    const GridGeom g = bgeom(a, P);
+    const int n = 1 + blockIdx.x * blockDim.y + threadIdx.y, k = threadIdx.x;
+    if (n > g.nf || k >= 2 * GPM_NGC) return;
+    double* ub = u + 4 * P.off;
+    const bool right = k >= GPM_NGC;
+    const int j = right ? k - GPM_NGC : k;
+    const int l = right ? g.lf + 1 + j : -j;
+    double* dst = ub + 4 * cidx(g, l, n);
+    if (g.bc_type == 17) {
+        const double* src = ub + 4 * cidx(g, right ? g.lf : 1, n);
+        for (int v = 0; v < 4; v++) dst[v] = src[v];
+    } else if (g.bc_type == 18) {
+        const double* src = ub + 4 * cidx(g, right ? 1 + j : g.lf - j, n);
+        for (int v = 0; v < 4; v++) dst[v] = src[v];
+    } else if (g.bc_type == 20) {
+        const double* src = ub + 4 * cidx(g, right ? g.lf - j : 1 + j, n);
+        dst[0] = src[0]; dst[1] = -src[1]; dst[2] = src[2]; dst[3] = src[3];
+    }
+}
+
+__global__ void kb_bc_y(BatchArgs a, double* __restrict__ u) {
+    const BProb P = a.prob[blockIdx.y];
+    const GridGeom g = bgeom(a, P);
+    const int l = (int)(blockIdx.x * blockDim.y + threadIdx.y) - 3, k = threadIdx.x;
+    if (l > g.lf + GPM_NGC || k >= 2 * GPM_NGC) return;
+    double* ub = u + 4 * P.off;
+    const bool top = k >= GPM_NGC;
+    const int j = top ? k - GPM_NGC : k;
+    const int n = top ? g.nf + 1 + j : -j;
+    double* dst = ub + 4 * cidx(g, l, n);
+    if (g.bc_type == 17) {
+        const double* src = ub + 4 * cidx(g, l, top ? g.nf : 1);
+        for (int v = 0; v < 4; v++) dst[v] = src[v];
+    } else if (g.bc_type == 18) {
+        const double* src = ub + 4 * cidx(g, l, top ? 1 + j : g.nf - j);
+        for (int v = 0; v < 4; v++) dst[v] = src[v];
+    } else if (g.bc_type == 20) {
+        const double* src = ub + 4 * cidx(g, l, top ? g.nf - j : 1 + j);
+        dst[0] = src[0]; dst[1] = src[1]; dst[2] = -src[2]; dst[3] = src[3];
+    }
+}
+
+static int g_max_nx = 0;  // set by the batch host code before launches (largest nx/ny of the batch)
+
+void blaunch_bc(const BatchArgs& a, double* u, cudaStream_t s) {
+    const dim3 blk(8, 32);
+    kb_bc_x<<<dim3((g_max_nx + 31) / 32, a.nprob), blk, 0, s>>>(a, u);
+    kb_bc_y<<<dim3((g_max_nx + 31) / 32, a.nprob), blk, 0, s>>>(a, u);
+}
+
+// Face tiles of every problem: a persistent CTA walks the tile list.  Tile
+// shape TXB x TYB is a template parameter chosen by the autotuner.
+template <int DIR, int NP, int NGP, int HXB>
+__device__ __forceinline__ void face_tile_b(const GpWeights& w, int o, const Cell* tile, int tx, int ty, double* F) {
+    constexpr int FL = DIR == 0 ? 2 : 1;
+    constexpr int FH = DIR == 0 ? 0 : 3;
+    double uL[NGP][4], uR[NGP][4];
+    {
+        Cell q[NP];
+#pragma unroll
+        for (int m = 0; m < NP; m++) q[m] = tile[(ty + st_oy(m)) * HXB + tx + st_ox(m)];
+        gp_recon<NP, NGP>(&w.zt[o][FL][0][0], q, uL);
+    }
+    {
+        constexpr int hx = DIR == 0 ? 1 : 0, hy = DIR == 0 ? 0 : 1;
+        Cell q[NP];
+#pragma unroll
+        for (int m = 0; m < NP; m++) q[m] = tile[(ty + hy + st_oy(m)) * HXB + tx + hx + st_ox(m)];
+        gp_recon<NP, NGP>(&w.zt[o][FH][0][0], q, uR);
+    }
+    quad_flux<DIR, NGP>(uL, uR, w.gw, F);
+}
+
+template <int TXB, int TYB, int NGP, int ORD>
+__global__ void __launch_bounds__(TXB* TYB) kb_flux(BatchArgs a) {
+    constexpr int HXB = TXB + 5, HYB = TYB + 5;
+    __shared__ Cell tile[HXB * HYB];
+    const int tid = threadIdx.y * TXB + threadIdx.x;
+    for (int item = blockIdx.x; item < a.nftiles; item += gridDim.x) {
+        const int4 it = a.ftiles[item];
+        const BProb P = a.prob[it.x];
+        const GridGeom g = bgeom(a, P);
+        const GpWeights& w = a.wtab[P.wc];
+        const double* ub = a.uin + 4 * P.off;
+        __syncthreads();  // the previous tile's faces are done with the buffer
+        for (int i = tid; i < HXB * HYB; i += TXB * TYB) {
+            const int cy = i / HXB, cx = i - cy * HXB;
+            const int l = it.z - 2 + cx, n = it.w - 2 + cy;
+            if (l >= -3 && l <= g.lf + 4 && n >= -3 && n <= g.nf + 4) tile[i] = ld_cell(ub + 4 * cidx(g, l, n));
+        }
+        __syncthreads();
+        const int l = it.z + threadIdx.x, n = it.w + threadIdx.y;
+        if (l > g.lf || n > g.nf) continue;
+        double F[4];
+        if (it.y == 0) face_tile_b<0, np_of(ORD), NGP, HXB>(w, ORD / 2, tile, threadIdx.x + 2, threadIdx.y + 2, F);
+        else face_tile_b<1, np_of(ORD), NGP, HXB>(w, ORD / 2, tile, threadIdx.x + 2, threadIdx.y + 2, F);
+        st_cell((it.y == 0 ? a.fx : a.fy) + 4 * (P.off + (long long)cidx(g, l, n)), Cell{F[0], F[1], F[2], F[3]});
+    }
+}
+
+static int g_sms = 0;
+static int sm_count() {
+    if (!g_sms) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    return g_sms;
+}
+
+template <int TXB, int TYB, int NGP>
+static void blaunch_flux_t(const BatchArgs& a, cudaStream_t s) {
+    const int grid = a.nftiles < sm_count() * 4 ? a.nftiles : sm_count() * 4;
+    const dim3 blk(TXB, TYB);
+    if (a.mord == 5) kb_flux<TXB, TYB, NGP, 5><<<grid, blk, 0, s>>>(a);
+    else if (a.mord == 3) kb_flux<TXB, TYB, NGP, 3><<<grid, blk, 0, s>>>(a);
+    else kb_flux<TXB, TYB, NGP, 1><<<grid, blk, 0, s>>>(a);
+}
+
+template <int NGP>
+static void blaunch_flux_n(const BatchArgs& a, cudaStream_t s) {
+    switch (a.tile) {
+    case 0: blaunch_flux_t<32, 8, NGP>(a, s); break;
+    case 1: blaunch_flux_t<32, 4, NGP>(a, s); break;
+    case 2: blaunch_flux_t<16, 16, NGP>(a, s); break;
+    default: blaunch_flux_t<64, 4, NGP>(a, s); break;
+    }
+}
+
+void blaunch_flux(const BatchArgs& a, cudaStream_t s) {
+    switch (a.ngp) {
+    case 1: blaunch_flux_n<1>(a, s); break;
+    case 2: blaunch_flux_n<2>(a, s); break;
+    case 3: blaunch_flux_n<3>(a, s); break;
+    case 4: blaunch_flux_n<4>(a, s); break;
+    default: blaunch_flux_n<5>(a, s); break;
+    }
+}
+
+__device__ __forceinline__ void list_append2(bool flag, int2* __restrict__ list, int* __restrict__ count, int2 value) {
+    const unsigned act = __activemask();
+    const unsigned m = __ballot_sync(act, flag);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(act) - 1;
+    int base = 0;
+    if (lane == leader) base = atomicAdd(count, __popc(m));
+    base = __shfl_sync(act, base, leader);
+    if (flag) list[base + __popc(m & ((1u << lane) - 1))] = value;
+}
+
+// First-pass update + DETECTION: persistent over blocks of 256 interior cells.
+__global__ void __launch_bounds__(256) kb_update(BatchArgs a) {
+    for (int item = blockIdx.x; item < a.ncblocks; item += gridDim.x) {
+        const int2 it = a.cblocks[item];
+        const BProb P = a.prob[it.x];
+        const GridGeom g = bgeom(a, P);
+        const int k = it.y + threadIdx.x;
+        bool trb = false;
+        int cl = 0;
+        if (k < g.lf * g.nf) {
+            const int l = 1 + k % g.lf, n = 1 + k / g.lf;
+            const size_t c = cidx(g, l, n);
+            const double* ub = a.uin + 4 * P.off;
+            const Cell uo = cell_update(g, ub, a.fx + 4 * P.off, a.fy + 4 * P.off, c, a.sc[it.x].qx, a.sc[it.x].qy);
+            st_cell(a.uout + 4 * (P.off + (long long)c), uo);
+            if (a.method == 2 && g.mord > 1)
+                trb = mood_troubled(uo, ub + 4 * c, g.nx, g, a.wtab[P.wc].d2x, a.wtab[P.wc].d2y);
+            cl = (int)c;
+        }
+        list_append2(trb, a.tlist[0], &a.ntrb[0], make_int2(it.x, cl));
+    }
+}
+
+void blaunch_update(const BatchArgs& a, cudaStream_t s) {
+    const int grid = a.ncblocks < sm_count() * 8 ? a.ncblocks : sm_count() * 8;
+    kb_update<<<grid, 256, 0, s>>>(a);
+}
+
+// One MOOD pass over every problem's list: cascade, the troubled cells' faces,
+// then their 5-point crosses.  Each kernel returns at once on an empty list,
+// so a captured graph holds a fixed number of passes at almost no cost.
+__global__ void kb_mood_mark(BatchArgs a, int cur) {
+    const int nt = a.ntrb[cur];
+    if (nt == 0) return;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
+        const int2 e = a.tlist[cur][i];
+        int8_t* o = a.order + a.prob[e.x].off + e.y;
+        const int v = *o;
+        *o = (int8_t)(v == 3 ? 1 : (v > 3 ? 3 : v));
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.ntrb[cur ^ 1] = 0;
+        a.ntrb[2] += 1;  // pass epoch for the de-duplication stamps
+    }
+}
+
+template <int NGP>
+__global__ void __launch_bounds__(128) kb_mood_faces(BatchArgs a, int cur) {
+    const int nt = a.ntrb[cur];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * nt; i += gridDim.x * blockDim.x) {
+        const int2 e = a.tlist[cur][i >> 2];
+        const BProb P = a.prob[e.x];
+        StageArgs sa;
+        sa.g = bgeom(a, P);
+        sa.uin = a.uin + 4 * P.off;
+        sa.fx = a.fx + 4 * P.off;
+        sa.fy = a.fy + 4 * P.off;
+        sa.order = a.order + P.off;
+        const GpWeights& w = a.wtab[P.wc];
+        const size_t c = (size_t)e.y;
+        const int f = i & 3;
+        if ((f & 1) == 0) face_any_order<0, NGP>(sa, w, f == 0 ? c - 1 : c);
+        else face_any_order<1, NGP>(sa, w, f == 1 ? c - sa.g.nx : c);
+    }
+}
+
+__global__ void __launch_bounds__(256) kb_mood_cells(BatchArgs a, int cur) {
+    const int nt = a.ntrb[cur];
+    if (nt == 0) return;
+    const unsigned epoch = (unsigned)a.ntrb[2];
+    const int nxt = cur ^ 1;
+    const int total = 5 * nt;
+    const int stride = gridDim.x * blockDim.x;
+    const int lim = ((total + stride - 1) / stride) * stride;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lim; i += stride) {
+        bool trb = false;
+        int2 val = make_int2(0, 0);
+        if (i < total) {
+            const int2 e = a.tlist[cur][i / 5];
+            const BProb P = a.prob[e.x];
+            const GridGeom g = bgeom(a, P);
+            const size_t t = (size_t)e.y;
+            const int k = i % 5;
+            const size_t c = k == 0 ? t - g.nx : k == 1 ? t - 1 : k == 2 ? t : k == 3 ? t + 1 : t + g.nx;
+            const int l = (int)(c % (size_t)g.nx) - 3, n = (int)(c / (size_t)g.nx) - 3;
+            if (l >= 1 && l <= g.lf && n >= 1 && n <= g.nf &&
+                atomicExch(&a.stamp[P.off + (long long)c], epoch) != epoch) {
+                const double* ub = a.uin + 4 * P.off;
+                const Cell uo = cell_update(g, ub, a.fx + 4 * P.off, a.fy + 4 * P.off, c, a.sc[e.x].qx, a.sc[e.x].qy);
+                st_cell(a.uout + 4 * (P.off + (long long)c), uo);
+                if (a.order[P.off + (long long)c] > 1)
+                    trb = mood_troubled(uo, ub + 4 * c, g.nx, g, a.wtab[P.wc].d2x, a.wtab[P.wc].d2y);
+                val = make_int2(e.x, (int)c);
+            }
+        }
+        list_append2(trb, a.tlist[nxt], &a.ntrb[nxt], val);
+    }
+}
+
+void blaunch_mood_pass(const BatchArgs& a, int cur, cudaStream_t s) {
+    const int g = sm_count() * 4;
+    kb_mood_mark<<<g, 256, 0, s>>>(a, cur);
+    switch (a.ngp) {
+    case 1: kb_mood_faces<1><<<g, 128, 0, s>>>(a, cur); break;
+    case 2: kb_mood_faces<2><<<g, 128, 0, s>>>(a, cur); break;
+    case 3: kb_mood_faces<3><<<g, 128, 0, s>>>(a, cur); break;
+    case 4: kb_mood_faces<4><<<g, 128, 0, s>>>(a, cur); break;
+    default: kb_mood_faces<5><<<g, 128, 0, s>>>(a, cur); break;
+    }
+    kb_mood_cells<<<g, 256, 0, s>>>(a, cur);
+}
+
+// The batch's whole MOOD loop in one cooperative launch (see k_mood_loop):
+// passes run until every problem's list is empty.  ntrb[2] is the stamp epoch,
+// ntrb[4] the detected-cell total, ntrb[5] the pass count of the last stage.
+template <int NGP>
+__global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar, int max_pass) {
+    const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    int cur = 0, pass = 1;
+    for (;;) {
+        const int nt = *(volatile int*)&a.ntrb[cur];
+        if (nt == 0) break;
+        if (pass >= max_pass) {
+            if (gtid == 0) a.ntrb[3] = 1;
+            break;
+        }
+        pass++;
+        for (int i = gtid; i < nt; i += gstride) {
+            const int2 e = a.tlist[cur][i];
+            int8_t* o = a.order + a.prob[e.x].off + e.y;
+            const int v = *o;
+            *o = (int8_t)(v == 3 ? 1 : (v > 3 ? 3 : v));
+        }
+        if (gtid == 0) {
+            a.ntrb[cur ^ 1] = 0;
+            a.ntrb[2] += 1;
+            a.ntrb[4] += nt;
+        }
+        if (!grid_sync(bar)) return;
+        for (int i = gtid; i < 4 * nt; i += gstride) {
+            const int2 e = a.tlist[cur][i >> 2];
+            const BProb P = a.prob[e.x];
+            StageArgs sa;
+            sa.g = bgeom(a, P);
+            sa.uin = a.uin + 4 * P.off;
+            sa.fx = a.fx + 4 * P.off;
+            sa.fy = a.fy + 4 * P.off;
+            sa.order = a.order + P.off;
+            const GpWeights& w = a.wtab[P.wc];
+            const size_t c = (size_t)e.y;
+            const int f = i & 3;
+            if ((f & 1) == 0) face_any_order<0, NGP>(sa, w, f == 0 ? c - 1 : c);
+            else face_any_order<1, NGP>(sa, w, f == 1 ? c - sa.g.nx : c);
+        }
+        if (!grid_sync(bar)) return;
+        const unsigned epoch = (unsigned)*(volatile int*)&a.ntrb[2];
+        const int nxt = cur ^ 1, total = 5 * nt;
+        const int lim = ((total + gstride - 1) / gstride) * gstride;
+        for (int i = gtid; i < lim; i += gstride) {
+            bool trb = false;
+            int2 val = make_int2(0, 0);
+            if (i < total) {
+                const int2 e = a.tlist[cur][i / 5];
+                const BProb P = a.prob[e.x];
+                const GridGeom g = bgeom(a, P);
+                const size_t t = (size_t)e.y;
+                const int k = i % 5;
+                const size_t c = k == 0 ? t - g.nx : k == 1 ? t - 1 : k == 2 ? t : k == 3 ? t + 1 : t + g.nx;
+                const int l = (int)(c % (size_t)g.nx) - 3, n = (int)(c / (size_t)g.nx) - 3;
+                if (l >= 1 && l <= g.lf && n >= 1 && n <= g.nf &&
+                    atomicExch(&a.stamp[P.off + (long long)c], epoch) != epoch) {
+                    const double* ub = a.uin + 4 * P.off;
+                    const Cell uo =
+                        cell_update(g, ub, a.fx + 4 * P.off, a.fy + 4 * P.off, c, a.sc[e.x].qx, a.sc[e.x].qy);
+                    st_cell(a.uout + 4 * (P.off + (long long)c), uo);
+                    if (a.order[P.off + (long long)c] > 1)
+                        trb = mood_troubled(uo, ub + 4 * c, g.nx, g, a.wtab[P.wc].d2x, a.wtab[P.wc].d2y);
+                    val = make_int2(e.x, (int)c);
+                }
+            }
+            list_append2(trb, a.tlist[nxt], &a.ntrb[nxt], val);
+        }
+        if (!grid_sync(bar)) return;
+        cur ^= 1;
+    }
+    if (gtid == 0) a.ntrb[5] = pass;
+}
+
+template <int NGP>
+static int blaunch_mood_loop_n(const BatchArgs& a, GridBar* bar, int max_pass, cudaStream_t s) {
+    static int grid = 0;
+    if (!grid) {
+        int occ = 0;
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kb_mood_loop<NGP>, 256, 0);
+        grid = sm_count() * (occ > 0 ? occ : 1);
+    }
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(grid);
+    cfg.blockDim = dim3(256);
+    cfg.stream = s;
+    cudaLaunchAttribute attr;
+    attr.id = cudaLaunchAttributeCooperative;
+    attr.val.cooperative = 1;
+    cfg.attrs = &attr;
+    cfg.numAttrs = 1;
+    return cudaLaunchKernelEx(&cfg, kb_mood_loop<NGP>, a, bar, max_pass) == cudaSuccess ? 0 : -1;
+}
+
+int blaunch_mood_loop(const BatchArgs& a, GridBar* bar, int max_pass, cudaStream_t s) {
+    switch (a.ngp) {
+    case 1: return blaunch_mood_loop_n<1>(a, bar, max_pass, s);
+    case 2: return blaunch_mood_loop_n<2>(a, bar, max_pass, s);
+    case 3: return blaunch_mood_loop_n<3>(a, bar, max_pass, s);
+    case 4: return blaunch_mood_loop_n<4>(a, bar, max_pass, s);
+    default: return blaunch_mood_loop_n<5>(a, bar, max_pass, s);
+    }
+}
+
+// After the last captured pass: a non-empty list means the stage hit the cap.
+__global__ void kb_leftover(BatchArgs a, int cur) {
+    if (a.ntrb[cur] != 0) a.ntrb[3] = 1;
+}
+void blaunch_leftover(const BatchArgs& a, int cur, cudaStream_t s) { kb_leftover<<<1, 1, 0, s>>>(a, cur); }
+
+// Per-problem CFL minimum: every block of padded cells belongs to one problem.
+__device__ __forceinline__ void bdt_reduce(double v, BScal* sc) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+    __shared__ double wmin[32];
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    __syncthreads();
+    if (lane == 0) wmin[wid] = v;
+    __syncthreads();
+    if (wid == 0) {
+        v = lane < (int)(blockDim.x >> 5) ? wmin[lane] : 1.0e30;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v = fmin(v, __shfl_xor_sync(0xffffffffu, v, o));
+        if (lane == 0 && v > 0.0 && v < 1.0e30) atomicMin(&sc->dtmin_bits, (unsigned long long)__double_as_longlong(v));
+    }
+}
+
+__global__ void __launch_bounds__(256) kb_combine(BatchArgs a, const double* __restrict__ x, double* __restrict__ y,
+                                                  double ca, double cb, int with_cfl, int only_cfl) {
+    for (int item = blockIdx.x; item < a.npblocks; item += gridDim.x) {
+        const int2 it = a.pblocks[item];
+        const BProb P = a.prob[it.x];
+        const int k = it.y + threadIdx.x;
+        double v = 1.0e30;
+        if (k < P.nx * P.ny) {
+            const long long c = P.off + k;
+            if (only_cfl) {
+                v = cell_dt(ld_cell(x + 4 * c), P.dx, P.dy);
+            } else {
+                const Cell p = ld_cell(x + 4 * c);
+                const Cell q = ld_cell_cg(y + 4 * c);
+                Cell o;
+                o.r = ca * p.r + cb * q.r;
+                o.mx = ca * p.mx + cb * q.mx;
+                o.my = ca * p.my + cb * q.my;
+                o.e = ca * p.e + cb * q.e;
+                st_cell(y + 4 * c, o);
+                if (with_cfl) v = cell_dt(o, P.dx, P.dy);
+            }
+        }
+        if (with_cfl || only_cfl) bdt_reduce(v, &a.sc[it.x]);
+    }
+}
+
+void blaunch_combine(const BatchArgs& a, const double* x, double* y, double ca, double cb, int with_cfl, cudaStream_t s) {
+    const int grid = a.npblocks < sm_count() * 8 ? a.npblocks : sm_count() * 8;
+    kb_combine<<<grid, 256, 0, s>>>(a, x, y, ca, cb, with_cfl, 0);
+}
+
+void blaunch_cfl(const BatchArgs& a, const double* u, cudaStream_t s) {
+    const int grid = a.npblocks < sm_count() * 8 ? a.npblocks : sm_count() * 8;
+    kb_combine<<<grid, 256, 0, s>>>(a, u, nullptr, 0.0, 0.0, 1, 1);
+}
+
+__global__ void kb_dt_finalize(BatchArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= a.nprob) return;
+    BScal& sc = a.sc[i];
+    double dt = __longlong_as_double((long long)sc.dtmin_bits);
+    dt = dt * sc.cfl;
+    const double dtfinal = sc.tmax - sc.t;
+    if (dt > dtfinal) dt = dtfinal;
+    sc.dt = dt;
+    sc.qx = dt / a.prob[i].dx;
+    sc.qy = dt / a.prob[i].dy;
+    sc.dtmin_bits = (unsigned long long)__double_as_longlong(1.0e30);
+    if (!(dt > 0.0) || is_nan(dt)) sc.status |= GPM_STATUS_DT;
+}
+
+__global__ void kb_advance_t(BatchArgs a) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < a.nprob) a.sc[i].t = a.sc[i].t + a.sc[i].dt;
+}
+
+void blaunch_dt_finalize(const BatchArgs& a, cudaStream_t s) { kb_dt_finalize<<<(a.nprob + 127) / 128, 128, 0, s>>>(a); }
+void blaunch_advance_t(const BatchArgs& a, cudaStream_t s) { kb_advance_t<<<(a.nprob + 127) / 128, 128, 0, s>>>(a); }
+
+void batch_set_max_nx(int nx) { g_max_nx = nx; }
+
+const BatchTable batch_table = {blaunch_bc,      blaunch_flux,        blaunch_update,    blaunch_mood_pass,
+                                blaunch_leftover, blaunch_combine,     blaunch_cfl,       blaunch_dt_finalize,
+                                blaunch_advance_t, blaunch_mood_loop};
 
 }  // namespace GPM_NS

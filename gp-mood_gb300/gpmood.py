@@ -95,6 +95,15 @@ SIGNATURES = {
     "gpmood_probe_fp64": ([_DP], C.c_int),
     "gpmood_time_stepping_noalloc": ([C.POINTER(Params), C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                       C.c_void_p], C.c_int),
+    "gpmood_batch_create": ([C.POINTER(Params), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
+                             C.POINTER(C.c_void_p)], C.c_int),
+    "gpmood_batch_destroy": ([C.c_void_p], None),
+    "gpmood_batch_set_state": ([C.c_void_p, C.c_int, _DP, C.c_double], C.c_int),
+    "gpmood_batch_get_state": ([C.c_void_p, C.c_int, _DP, _DP], C.c_int),
+    "gpmood_batch_advance": ([C.c_void_p, C.c_int], C.c_int),
+    "gpmood_batch_autotune": ([C.c_void_p, C.POINTER(C.c_int), _DP], C.c_int),
+    "gpmood_batch_stats": ([C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
+                            C.POINTER(C.c_longlong), C.POINTER(C.c_int)], C.c_int),
 }
 
 _lib: C.CDLL | None = None
@@ -320,3 +329,75 @@ class Solver:
         self._check(self.lib.gpmood_nn_harvest(self._h, C.c_void_p(d_x or None), C.c_void_p(d_y or None),
                                                int(capacity), float(keep_negative), int(seed) & 0xFFFFFFFF,
                                                C.c_void_p(d_count or None)))
+
+
+class Batch:
+    """Many independent problems of uneven size stepped together (gpmood_batch_*)."""
+
+    def __init__(self, sizes, params: Params | None = None, **kw):
+        self.lib = load_library()
+        self.p = params if params is not None else default_params(**kw)
+        self.sizes = [(int(a), int(b)) for a, b in sizes]
+        n = len(self.sizes)
+        lf = (C.c_int * n)(*[a for a, _ in self.sizes])
+        nf = (C.c_int * n)(*[b for _, b in self.sizes])
+        h = C.c_void_p()
+        rc = self.lib.gpmood_batch_create(C.byref(self.p), n, lf, nf, C.byref(h))
+        if rc != 0:
+            raise GpmoodError(rc, self._err())
+        self._h = h
+
+    def _err(self) -> str:
+        buf = C.create_string_buffer(512)
+        self.lib.gpmood_last_error(None, buf, 512)
+        return buf.value.decode(errors="replace")
+
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            raise GpmoodError(rc, self._err())
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.gpmood_batch_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def set_state(self, i: int, U: np.ndarray, t: float = 0.0) -> None:
+        lf, nf = self.sizes[i]
+        if U.shape != (nf + 2 * NGC, lf + 2 * NGC, 4) or U.dtype != np.float64 or not U.flags.c_contiguous:
+            raise ValueError("state has the wrong shape or dtype")
+        self._check(self.lib.gpmood_batch_set_state(self._h, i, _dp(U), t))
+
+    def get_state(self, i: int):
+        lf, nf = self.sizes[i]
+        U = np.empty((nf + 2 * NGC, lf + 2 * NGC, 4))
+        t = C.c_double()
+        self._check(self.lib.gpmood_batch_get_state(self._h, i, _dp(U), C.byref(t)))
+        return U, t.value
+
+    def advance(self, nsteps: int) -> None:
+        self._check(self.lib.gpmood_batch_advance(self._h, int(nsteps)))
+
+    def autotune(self):
+        k = C.c_int()
+        ms = np.zeros(4)
+        self._check(self.lib.gpmood_batch_autotune(self._h, C.byref(k), _dp(ms)))
+        return k.value, ms
+
+    def stats(self) -> dict:
+        vals = [C.c_longlong() for _ in range(4)]
+        g = C.c_int()
+        self._check(self.lib.gpmood_batch_stats(self._h, *[C.byref(v) for v in vals], C.byref(g)))
+        return {"interior_cells": vals[0].value, "steps": vals[1].value, "detected": vals[2].value,
+                "status": vals[3].value, "graphed": g.value}

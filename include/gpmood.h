@@ -75,7 +75,8 @@ typedef struct gpmood_params {
     int bc_type;          /* GPMOOD_NEUMANN/PERIODIC/REFLECTIVE/DMR    :45 */
     int nmax;             /* step cap of the time loop                 :42 */
     int fp_mode;          /* GPMOOD_FP_EXACT or GPMOOD_FP_FAST */
-    int max_mood_iters;   /* MOOD passes allowed per stage before GPMOOD_E_MOOD_CAP */
+    int max_mood_iters;   /* MOOD passes allowed per stage before GPMOOD_E_MOOD_CAP; 0 (default)
+                             allows 2*lf*nf+2, more than a terminating loop can take */
     int nsteps_with_no_nn;/* gate off for the first steps (global_variables.f90:97) */
 } gpmood_params;
 
@@ -172,6 +173,31 @@ int  gpmood_time_stepping_dev(gpmood_ctx* ctx, double* d_uin, double* d_uout,
  * synchronous at return.  Errors: gpmood_last_error(NULL, ...). */
 int  gpmood_time_stepping_noalloc(const gpmood_params* p, double* d_uin, double* d_uout,
                                   double t, double dt, void* stream);
+
+/* ---- many independent problems of uneven size (one GPU) ---- */
+
+/* No counterpart in the reference (which runs one problem per process).  A
+ * batch steps nprob problems that share the knobs of p (method GP_MOOD or
+ * GP_SE; Neumann, periodic or reflective BCs), problem i on lf[i] x nf[i]
+ * cells of [0,Lx]x[0,Ly], each with its own CFL time step.  Every phase of an
+ * RK stage is one persistent launch over all problems and the MOOD loop one
+ * cooperative launch per stage; a step is replayed from a CUDA graph. */
+typedef struct gpmood_batch gpmood_batch;
+int  gpmood_batch_create(const gpmood_params* p, int nprob, const int* lf, const int* nf,
+                         gpmood_batch** out);
+void gpmood_batch_destroy(gpmood_batch* b);
+/* Problem i's state, Fortran layout of (lf[i]+8)*(nf[i]+8)*4 doubles, and time. */
+int  gpmood_batch_set_state(gpmood_batch* b, int i, const double* u_host, double t);
+int  gpmood_batch_get_state(gpmood_batch* b, int i, double* u_host, double* t);
+/* nsteps steps of every problem (Setdt + time_stepping + t += dt each). */
+int  gpmood_batch_advance(gpmood_batch* b, int nsteps);
+/* Time each face-tile shape on this batch and keep the fastest: *tile gets its
+ * index, ms_per_tile[4] (may be NULL) the measured times. */
+int  gpmood_batch_autotune(gpmood_batch* b, int* tile, double* ms_per_tile);
+/* Interior cells of all problems, steps taken, detected cells (all steps),
+ * status bits, and 1 if steps replay a CUDA graph (-1: eager launches). */
+int  gpmood_batch_stats(const gpmood_batch* b, long long* interior_cells, long long* steps,
+                        long long* detected, long long* status, int* graphed);
 
 /* ---- measurement ---- */
 

@@ -43,7 +43,7 @@ def test_default_params_are_the_reference_knobs(pkg):
 
 @pytest.mark.parametrize("bad", [dict(mord=7), dict(ngp=6), dict(num_flux=103), dict(integrator=12),
                                  dict(bc_type=19), dict(lf=2), dict(method=200), dict(fp_mode=3),
-                                 dict(max_mood_iters=0), dict(cfl=0.0)])
+                                 dict(max_mood_iters=-1), dict(cfl=0.0)])
 def test_invalid_knobs_rejected(pkg, bad):
     with pytest.raises(pkg.GpmoodError) as e:
         pkg.Solver(**bad)

@@ -153,3 +153,25 @@ def test_gp_se_mode(pkg, oracle):
         Ug = np.empty_like(U)
         s.time_stepping(U, Ug, 0.0, dt)
     assert nan_equal(Ug, Ur)
+
+
+def test_mood_cap_is_an_error_and_the_context_survives(pkg, oracle):
+    """A MOOD loop stopped by max_mood_iters returns GPMOOD_E_MOOD_CAP (no hang,
+    no fault); the same problem then steps normally with the default cap."""
+    ic, lf, nf, kn = CASES["rp2d3"]
+    p = _oracle_params(oracle, lf, nf, kn)
+    U = oracle.initial_condition(p, ic)
+    dt = oracle.setdt(p, U, p.tmax)
+    with _solver(pkg, lf, nf, pkg.FP_EXACT, dict(kn, max_mood_iters=1)) as s:
+        out = np.empty_like(U)
+        with pytest.raises(pkg.GpmoodError) as e:
+            s.time_stepping(U, out, 0.0, dt)
+        assert e.value.code == -3
+        assert s.counters().status_flags & 2
+    ref = np.empty_like(U)
+    oracle.Stepper(p).time_stepping(U.copy(), ref, 0.0, dt)
+    with _solver(pkg, lf, nf, pkg.FP_EXACT, kn) as s:
+        out = np.empty_like(U)
+        s.time_stepping(U, out, 0.0, dt)
+        assert s.counters().max_passes_stage > 1
+    assert nan_equal(out, ref)
