@@ -2,12 +2,17 @@
 
 Package layout:
   csrc/        CUDA kernels (sm_103a) and the C ABI of libgpmood.so
-  gpmood.py    ctypes binding mirroring the reference's time_stepping/Setdt/Boundary_C
+  gpmood.py    ctypes binding mirroring the reference's time_stepping/Setdt/Boundary_C,
+               plus the batched (Batch) and adjoint (Adjoint) entry points
+  adjoint.py   torch.autograd front end of the adjoint (imports torch on use)
+  nn_train.py  training of the a-priori MLP gate on the GPU kernels
   ic.py        initial conditions of the benchmark problems
   build.py     in-tree build of libgpmood.so
 """
 from .gpmood import (DMR, FP_EXACT, FP_FAST, GP_MOOD, GP_SE, HLLC, NEUMANN, NGC, NN_GP_MOOD, PERIODIC,
-                     REFLECTIVE, SSP_RK3, GpmoodError, Params, Solver, default_params, load_library, padded)
+                     REFLECTIVE, SSP_RK3, Adjoint, Batch, GpmoodError, Params, Solver, default_params, gp_weights,
+                     load_library, padded, probe_fp64)
 
 __all__ = ["DMR", "FP_EXACT", "FP_FAST", "GP_MOOD", "GP_SE", "HLLC", "NEUMANN", "NGC", "NN_GP_MOOD", "PERIODIC",
-           "REFLECTIVE", "SSP_RK3", "GpmoodError", "Params", "Solver", "default_params", "load_library", "padded"]
+           "REFLECTIVE", "SSP_RK3", "Adjoint", "Batch", "GpmoodError", "Params", "Solver", "default_params",
+           "gp_weights", "load_library", "padded", "probe_fp64"]

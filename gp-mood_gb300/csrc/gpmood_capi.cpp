@@ -517,6 +517,27 @@ int gpmood_get_state(gpmood_ctx* c, double* u_host, double* t, int* niter) {
     return 0;
 }
 
+int gpmood_set_state_dev(gpmood_ctx* c, const double* d_u, double t) {
+    if (!c || !d_u) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    CU(cudaMemcpyAsync(c->dU, d_u, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream));
+    int rc = set_time(c, t, 0.0);
+    if (rc) return rc;
+    CU(cudaStreamSynchronize(c->stream));
+    c->t = t;
+    c->niter = 0;
+    c->have_state = true;
+    c->dt_pending = false;
+    return 0;
+}
+
+int gpmood_get_state_dev(gpmood_ctx* c, double* d_u) {
+    if (!c || !d_u) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
+    CU(cudaMemcpyAsync(d_u, c->dU, state_bytes(c), cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
 int gpmood_get_orders(gpmood_ctx* c, signed char* orders) {
     if (!c || !orders) return fail(c, GPMOOD_E_ARG, "NULL argument");
     // CellGPO(1:lf, 1:nf): interior rows of the padded order array.
@@ -690,6 +711,262 @@ int gpmood_nn_adam(float* d_params, const float* d_grad, float* d_m, float* d_v,
         return fail(nullptr, GPMOOD_E_CUDA, "adam launch failed");
     cudaError_t e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) return fail(nullptr, GPMOOD_E_CUDA, "adam: %s", cudaGetErrorString(e));
+    return 0;
+}
+
+}  // extern "C"
+
+// ===========================================================================
+// Adjoint of the step with frozen MOOD order masks (adjoint.cu for the stage
+// VJP).  A step n -> n+1 with stage inputs X0 = U_n, X1, X2 is
+//   X1 = S0(X0),  X2 = 3/4 X0 + 1/4 S1(X1),  U_{n+1} = 1/3 X0 + 2/3 S2(X2)
+// (mod_SSP_RK3.f90:12-39), each S a Forward_Euler stage at its recorded
+// orders and the step's dt.  Backward:
+//   l2 = S2^T(2/3 l),  l1 = S1^T(1/4 l2),  l_n = 1/3 l + 3/4 l2 + S0^T(l1).
+#include "adjoint.h"
+
+struct gpmood_adjoint {
+    gpmood_ctx* c;
+    int nsteps, every, nck;
+    double *t, *dt;              // host, per step
+    int8_t* dOrd;                // nsteps x 3 x ncell frozen CellGPO
+    double* dCk;                 // nck checkpoints (U_{k*every})
+    double* dSeg;                // 3*every+1 stage inputs of one segment
+    double *dLam, *dLamB, *dTA, *dAcc, *dTmp, *dMu, *dFace;
+    DevScalars* dSc;             // the adjoint's own t, dt, qx, qy
+    DevScalars* hSc;             // pinned mirror
+};
+
+namespace {
+
+double* adj_state(gpmood_adjoint* a, double* base, int i) { return base + (size_t)i * a->c->ncell * 4; }
+
+int adj_set_time(gpmood_adjoint* a, int step) {
+    gpmood_ctx* c = a->c;
+    a->hSc->t = a->t[step];
+    a->hSc->dt = a->dt[step];
+    a->hSc->qx = a->dt[step] / c->g.dx;
+    a->hSc->qy = a->dt[step] / c->g.dy;
+    CU(cudaMemcpyAsync(a->dSc, a->hSc, 4 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    return 0;
+}
+
+// One Forward_Euler stage at frozen orders: Boundary_C(uin), fluxes at
+// min(CellGPO) per face, flux-difference update without DETECTION, Boundary_C(uout).
+void adj_frozen_stage(gpmood_adjoint* a, double* uin, double* uout, const int8_t* ord, int stage) {
+    gpmood_ctx* c = a->c;
+    const KernelTable& kt = *c->kt;
+    StageArgs sa = stage_args(c, uin, uout, stage, false);
+    sa.g.method = GPMOOD_GP_SE;  // no DETECTION
+    sa.order = const_cast<int8_t*>(ord);
+    sa.sc = a->dSc;
+    kt.bc(c->g, uin, a->dSc, stage, c->stream);
+    kt.flux_all(sa, c->w, c->stream);
+    kt.update_detect(sa, c->w, 0, c->stream);
+    kt.bc(c->g, uout, a->dSc, stage, c->stream);
+}
+
+const int8_t* adj_ord(const gpmood_adjoint* a, int step, int stage) {
+    return a->dOrd + ((size_t)step * 3 + stage) * a->c->ncell;
+}
+
+// Step `step` from x0 (its ghosts are refreshed in place) into next, keeping
+// the stage inputs X1, X2 in x1, x2.
+int adj_replay_step(gpmood_adjoint* a, int step, double* x0, double* x1, double* x2, double* next) {
+    gpmood_ctx* c = a->c;
+    int rc = adj_set_time(a, step);
+    if (rc) return rc;
+    adj_frozen_stage(a, x0, x1, adj_ord(a, step, 0), 0);
+    adj_frozen_stage(a, x1, x2, adj_ord(a, step, 1), 1);
+    c->kt->combine(c->g, x0, x2, 0.75, 0.25, 0, a->dSc, c->stream);
+    adj_frozen_stage(a, x2, next, adj_ord(a, step, 2), 2);
+    c->kt->combine(c->g, x0, next, 1. / 3, 2. / 3, 0, a->dSc, c->stream);
+    return check_launch(c, "adjoint replay");
+}
+
+// lam_in = S^T(lam_out) at the stage input x with the frozen orders of (step, stage).
+int adj_stage_vjp(gpmood_adjoint* a, int step, int stage, const double* x, const double* lam_out, double* lam_in) {
+    gpmood_ctx* c = a->c;
+    AdjArgs aa;
+    aa.g = c->g;
+    aa.u_in = x;
+    aa.order = adj_ord(a, step, stage);
+    aa.lam_out = lam_out;
+    aa.lam_in = lam_in;
+    aa.face_adj = a->dFace;
+    aa.mu_pad = a->dMu;
+    aa.qx = a->dt[step] / c->g.dx;
+    aa.qy = a->dt[step] / c->g.dy;
+    if (gpm_adj_stage(aa, c->w, c->stream)) return fail(c, GPMOOD_E_CUDA, "adjoint stage launch failed");
+    return 0;
+}
+
+void adj_free(gpmood_adjoint* a) {
+    if (!a) return;
+    delete[] a->t;
+    delete[] a->dt;
+    cudaFree(a->dOrd); cudaFree(a->dCk); cudaFree(a->dSeg);
+    cudaFree(a->dLam); cudaFree(a->dLamB); cudaFree(a->dTA); cudaFree(a->dAcc); cudaFree(a->dTmp);
+    cudaFree(a->dMu); cudaFree(a->dFace); cudaFree(a->dSc);
+    if (a->hSc) cudaFreeHost(a->hSc);
+    delete a;
+}
+
+}  // namespace
+
+extern "C" {
+
+int gpmood_adj_record(gpmood_ctx* c, int nsteps, int every, gpmood_adjoint** out) {
+    if (!c || !out) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    *out = nullptr;
+    if (nsteps < 1 || every < 1) return fail(c, GPMOOD_E_ARG, "nsteps and every must be >= 1");
+    if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
+    if (c->p.bc_type == GPMOOD_DMR)
+        return fail(c, GPMOOD_E_ARG, "adjoint: BC_type DMR (time-dependent inflow) is not supported");
+    gpmood_adjoint* a = new (std::nothrow) gpmood_adjoint();
+    if (!a) return fail(c, GPMOOD_E_ARG, "out of host memory");
+    a->c = c;
+    a->every = every;
+    a->nck = (nsteps + every - 1) / every;
+    a->t = new (std::nothrow) double[nsteps];
+    a->dt = new (std::nothrow) double[nsteps];
+    const size_t sb = state_bytes(c);
+    bool ok = a->t && a->dt;
+#define AALLOC(ptr, bytes) ok = ok && cudaMalloc((void**)&(ptr), (bytes)) == cudaSuccess
+    AALLOC(a->dOrd, (size_t)nsteps * 3 * c->ncell);
+    AALLOC(a->dCk, (size_t)a->nck * sb);
+    AALLOC(a->dSeg, (size_t)(3 * every + 1) * sb);
+    AALLOC(a->dLam, sb);
+    AALLOC(a->dLamB, sb);
+    AALLOC(a->dTA, sb);
+    AALLOC(a->dAcc, sb);
+    AALLOC(a->dTmp, sb);
+    AALLOC(a->dMu, sb);
+    AALLOC(a->dFace, 2 * c->ncell * 8 * GPM_MAXGP * sizeof(double));
+    AALLOC(a->dSc, sizeof(DevScalars));
+#undef AALLOC
+    ok = ok && cudaMallocHost((void**)&a->hSc, sizeof(DevScalars)) == cudaSuccess;
+    if (ok) {  // adjoint buffers keep zero ghosts for their whole life
+        cudaStream_t s = c->stream;
+        ok = cudaMemsetAsync(a->dLam, 0, sb, s) == cudaSuccess && cudaMemsetAsync(a->dLamB, 0, sb, s) == cudaSuccess &&
+             cudaMemsetAsync(a->dTA, 0, sb, s) == cudaSuccess && cudaMemsetAsync(a->dAcc, 0, sb, s) == cudaSuccess &&
+             cudaMemsetAsync(a->dTmp, 0, sb, s) == cudaSuccess && cudaMemsetAsync(a->dSc, 0, sizeof(DevScalars), s) == cudaSuccess &&
+             cudaStreamSynchronize(s) == cudaSuccess;
+        if (ok) memset(a->hSc, 0, sizeof(DevScalars));
+    }
+    if (!ok) {
+        adj_free(a);
+        return fail(c, GPMOOD_E_CUDA, "adjoint: allocation failed");
+    }
+    int done = 0;
+    for (int s = 0; s < nsteps; s++) {
+        if (s % every == 0) {
+            cudaError_t e = cudaMemcpyAsync(adj_state(a, a->dCk, s / every), c->dU, sb, cudaMemcpyDeviceToDevice, c->stream);
+            if (e != cudaSuccess) { adj_free(a); return fail(c, GPMOOD_E_CUDA, "adjoint checkpoint: %s", cudaGetErrorString(e)); }
+        }
+        int one = 0;
+        int rc = gpmood_advance(c, 1, &one);
+        if (rc) { adj_free(a); return rc; }
+        if (!one) break;  // tmax or nmax reached
+        a->t[s] = c->hSc->t;
+        a->dt[s] = c->hSc->dt;
+        cudaError_t e = cudaMemcpyAsync(a->dOrd + (size_t)s * 3 * c->ncell, c->dStageOrd, 3 * c->ncell,
+                                        cudaMemcpyDeviceToDevice, c->stream);
+        if (e != cudaSuccess) { adj_free(a); return fail(c, GPMOOD_E_CUDA, "adjoint orders: %s", cudaGetErrorString(e)); }
+        done++;
+    }
+    if (cudaStreamSynchronize(c->stream) != cudaSuccess) { adj_free(a); return fail(c, GPMOOD_E_CUDA, "adjoint record sync"); }
+    if (done == 0) { adj_free(a); return fail(c, GPMOOD_E_STATE, "adjoint: no step taken (t >= tmax)"); }
+    a->nsteps = done;
+    a->nck = (done + every - 1) / every;
+    *out = a;
+    return 0;
+}
+
+void gpmood_adj_destroy(gpmood_adjoint* a) { adj_free(a); }
+
+int gpmood_adj_info(const gpmood_adjoint* a, int* nsteps, double* t, double* dt) {
+    if (!a) return fail(nullptr, GPMOOD_E_ARG, "adjoint is NULL");
+    if (nsteps) *nsteps = a->nsteps;
+    if (t) memcpy(t, a->t, (size_t)a->nsteps * sizeof(double));
+    if (dt) memcpy(dt, a->dt, (size_t)a->nsteps * sizeof(double));
+    return 0;
+}
+
+int gpmood_adj_orders(const gpmood_adjoint* a, int step, int stage, signed char* orders_host) {
+    if (!a || !orders_host) return fail(a ? a->c : nullptr, GPMOOD_E_ARG, "NULL argument");
+    gpmood_ctx* c = a->c;
+    if (step < 0 || step >= a->nsteps || stage < 0 || stage > 2) return fail(c, GPMOOD_E_ARG, "step/stage out of range");
+    CU(cudaMemcpyAsync(orders_host, adj_ord(a, step, stage), c->ncell, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int gpmood_adj_replay(gpmood_adjoint* a, const double* d_u0, double* d_uN) {
+    if (!a || !d_u0 || !d_uN) return fail(a ? a->c : nullptr, GPMOOD_E_ARG, "NULL argument");
+    gpmood_ctx* c = a->c;
+    const size_t sb = state_bytes(c);
+    double *x0 = adj_state(a, a->dSeg, 0), *x1 = adj_state(a, a->dSeg, 1), *x2 = adj_state(a, a->dSeg, 2);
+    double* nx = adj_state(a, a->dSeg, 3);
+    CU(cudaMemcpyAsync(x0, d_u0, sb, cudaMemcpyDeviceToDevice, c->stream));
+    for (int s = 0; s < a->nsteps; s++) {
+        int rc = adj_replay_step(a, s, x0, x1, x2, nx);
+        if (rc) return rc;
+        double* tmp = x0;
+        x0 = nx;
+        nx = tmp;
+    }
+    CU(cudaMemcpyAsync(d_uN, x0, sb, cudaMemcpyDeviceToDevice, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int gpmood_adj_backward(gpmood_adjoint* a, const double* d_lamN, double* d_lam0) {
+    if (!a || !d_lamN || !d_lam0) return fail(a ? a->c : nullptr, GPMOOD_E_ARG, "NULL argument");
+    gpmood_ctx* c = a->c;
+    cudaStream_t st = c->stream;
+    const size_t sb = state_bytes(c);
+    const KernelTable& kt = *c->kt;
+    // U_N's ghosts are Boundary_C of its interior: fold their adjoint in.
+    CU(cudaMemcpyAsync(a->dMu, d_lamN, sb, cudaMemcpyDeviceToDevice, st));
+    CU(cudaMemsetAsync(a->dTmp, 0, sb, st));
+    if (gpm_adj_fold(c->g, a->dMu, a->dTmp, a->dLam, st)) return fail(c, GPMOOD_E_CUDA, "adjoint fold launch failed");
+    for (int seg = a->nck - 1; seg >= 0; seg--) {
+        const int s0 = seg * a->every, s1 = s0 + a->every < a->nsteps ? s0 + a->every : a->nsteps;
+        // recompute the segment's stage inputs from its checkpoint
+        CU(cudaMemcpyAsync(adj_state(a, a->dSeg, 0), adj_state(a, a->dCk, seg), sb, cudaMemcpyDeviceToDevice, st));
+        for (int s = s0; s < s1; s++) {
+            const int i = 3 * (s - s0);
+            int rc = adj_replay_step(a, s, adj_state(a, a->dSeg, i), adj_state(a, a->dSeg, i + 1),
+                                     adj_state(a, a->dSeg, i + 2), adj_state(a, a->dSeg, i + 3));
+            if (rc) return rc;
+        }
+        for (int s = s1 - 1; s >= s0; s--) {
+            const int i = 3 * (s - s0);
+            const double *x0 = adj_state(a, a->dSeg, i), *x1 = adj_state(a, a->dSeg, i + 1);
+            const double* x2 = adj_state(a, a->dSeg, i + 2);
+            CU(cudaMemcpyAsync(a->dTA, a->dLam, sb, cudaMemcpyDeviceToDevice, st));
+            kt.combine(c->g, a->dLam, a->dTA, 0.0, 2. / 3, 0, a->dSc, st);      // TA = 2/3 l
+            int rc = adj_stage_vjp(a, s, 2, x2, a->dTA, a->dLamB);             // l2
+            if (rc) return rc;
+            CU(cudaMemcpyAsync(a->dAcc, a->dLam, sb, cudaMemcpyDeviceToDevice, st));
+            kt.combine(c->g, a->dLamB, a->dAcc, 0.75, 1. / 3, 0, a->dSc, st);  // acc = 1/3 l + 3/4 l2
+            CU(cudaMemcpyAsync(a->dTA, a->dLamB, sb, cudaMemcpyDeviceToDevice, st));
+            kt.combine(c->g, a->dLamB, a->dTA, 0.0, 0.25, 0, a->dSc, st);     // TA = 1/4 l2
+            rc = adj_stage_vjp(a, s, 1, x1, a->dTA, a->dLamB);                 // l1
+            if (rc) return rc;
+            rc = adj_stage_vjp(a, s, 0, x0, a->dLamB, a->dTmp);                // S0^T(l1)
+            if (rc) return rc;
+            kt.combine(c->g, a->dAcc, a->dTmp, 1.0, 1.0, 0, a->dSc, st);      // l_s = acc + S0^T(l1)
+            double* tmp = a->dLam;
+            a->dLam = a->dTmp;
+            a->dTmp = tmp;
+            rc = check_launch(c, "adjoint step");
+            if (rc) return rc;
+        }
+    }
+    CU(cudaMemcpyAsync(d_lam0, a->dLam, sb, cudaMemcpyDeviceToDevice, st));
+    CU(cudaStreamSynchronize(st));
     return 0;
 }
 

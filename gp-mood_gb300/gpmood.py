@@ -104,6 +104,14 @@ SIGNATURES = {
     "gpmood_batch_autotune": ([C.c_void_p, C.POINTER(C.c_int), _DP], C.c_int),
     "gpmood_batch_stats": ([C.c_void_p, C.POINTER(C.c_longlong), C.POINTER(C.c_longlong), C.POINTER(C.c_longlong),
                             C.POINTER(C.c_longlong), C.POINTER(C.c_int)], C.c_int),
+    "gpmood_set_state_dev": ([C.c_void_p, C.c_void_p, C.c_double], C.c_int),
+    "gpmood_get_state_dev": ([C.c_void_p, C.c_void_p], C.c_int),
+    "gpmood_adj_record": ([C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_void_p)], C.c_int),
+    "gpmood_adj_destroy": ([C.c_void_p], None),
+    "gpmood_adj_info": ([C.c_void_p, C.POINTER(C.c_int), _DP, _DP], C.c_int),
+    "gpmood_adj_orders": ([C.c_void_p, C.c_int, C.c_int, C.POINTER(C.c_byte)], C.c_int),
+    "gpmood_adj_replay": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
+    "gpmood_adj_backward": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
 }
 
 _lib: C.CDLL | None = None
@@ -324,11 +332,78 @@ class Solver:
     def nn_features(self, d_x: int, d_const: int = 0) -> None:
         self._check(self.lib.gpmood_nn_features(self._h, C.c_void_p(d_x), C.c_void_p(d_const or None)))
 
+    def set_state_dev(self, d_u: int, t: float = 0.0) -> None:
+        self._check(self.lib.gpmood_set_state_dev(self._h, C.c_void_p(d_u), float(t)))
+
+    def get_state_dev(self, d_u: int) -> None:
+        self._check(self.lib.gpmood_get_state_dev(self._h, C.c_void_p(d_u)))
+
+    def adj_record(self, nsteps: int, every: int = 10) -> "Adjoint":
+        """Advance nsteps steps recording dt and the frozen order masks, with a
+        state checkpoint every ``every`` steps (gpmood_adj_record)."""
+        h = C.c_void_p()
+        self._check(self.lib.gpmood_adj_record(self._h, int(nsteps), int(every), C.byref(h)))
+        return Adjoint(self, h)
+
     def nn_harvest(self, d_x: int, d_y: int, capacity: int, keep_negative: float, seed: int, d_count: int) -> None:
         """Attach (d_x != 0) or detach (d_x == 0) training-sample buffers."""
         self._check(self.lib.gpmood_nn_harvest(self._h, C.c_void_p(d_x or None), C.c_void_p(d_y or None),
                                                int(capacity), float(keep_negative), int(seed) & 0xFFFFFFFF,
                                                C.c_void_p(d_count or None)))
+
+
+class Adjoint:
+    """A recording of steps with frozen MOOD order masks (gpmood_adj_*): frozen
+    replay and the vector-Jacobian product along the recorded trajectory.
+    Device arrays are passed as integer pointers to padded-layout float64 data."""
+
+    def __init__(self, solver: Solver, handle):
+        self.solver = solver
+        self.lib = solver.lib
+        self._h = handle
+        n = C.c_int()
+        self.lib.gpmood_adj_info(self._h, C.byref(n), None, None)
+        self.nsteps = n.value
+
+    def _check(self, rc: int) -> None:
+        if rc != 0:
+            raise GpmoodError(rc, self.solver._err(self.solver._h))
+
+    def close(self) -> None:
+        if getattr(self, "_h", None):
+            self.lib.gpmood_adj_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def info(self):
+        """(t, dt) of every recorded step."""
+        t = np.zeros(self.nsteps)
+        dt = np.zeros(self.nsteps)
+        self._check(self.lib.gpmood_adj_info(self._h, None, _dp(t), _dp(dt)))
+        return t, dt
+
+    def orders(self, step: int, stage: int) -> np.ndarray:
+        """Padded CellGPO (nf+8, lf+8) of RK stage ``stage`` of step ``step``."""
+        o = np.zeros(self.solver.shape[:2], dtype=np.int8)
+        self._check(self.lib.gpmood_adj_orders(self._h, int(step), int(stage), o.ctypes.data_as(C.POINTER(C.c_byte))))
+        return o
+
+    def replay(self, d_u0: int, d_uN: int) -> None:
+        self._check(self.lib.gpmood_adj_replay(self._h, C.c_void_p(d_u0), C.c_void_p(d_uN)))
+
+    def backward(self, d_lamN: int, d_lam0: int) -> None:
+        self._check(self.lib.gpmood_adj_backward(self._h, C.c_void_p(d_lamN), C.c_void_p(d_lam0)))
 
 
 class Batch:

@@ -115,3 +115,23 @@ def isentropic_vortex(lf: int, nf: int, lx: float = 10.0, ly: float = 10.0, beta
                 acc = acc + w[j] * w[i] * point(lxh * xg[i] + x, lyh * xg[j] + y)
         return (1. / (dx * dy)) * (acc * lxh * lyh)
     return _fill(lf, nf, lx, ly, fn)
+
+
+BATCH_SIZES = (64, 96, 128, 192, 256)
+
+
+def random_riemann(seed: int, sizes=BATCH_SIZES):
+    """One problem of the batched workload: a four-quadrant Riemann problem on
+    [0,1]^2 whose quadrant states (rho ~ U[0.1,2], p ~ U[0.02,2],
+    u, v ~ U[-1.5,1.5]), split point (~ U[0.3,0.8]^2) and square grid size
+    (uniform over ``sizes``) are drawn from numpy's PCG64 seeded with ``seed``."""
+    rng = np.random.default_rng(seed)
+    n = int(sizes[rng.integers(len(sizes))])
+    split = tuple(rng.uniform(0.3, 0.8, size=2))
+    states = []
+    for _ in range(4):
+        r = rng.uniform(0.1, 2.0)
+        u, v = rng.uniform(-1.5, 1.5, size=2)
+        p = rng.uniform(0.02, 2.0)
+        states.append((r, u, v, p))
+    return riemann4(n, n, split, states), n

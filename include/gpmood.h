@@ -146,6 +146,9 @@ int  gpmood_time_stepping(gpmood_ctx* ctx, const double* uin_host, double* uout_
 int  gpmood_set_state(gpmood_ctx* ctx, const double* u_host, double t);
 /* Download state, time and step count (any pointer may be NULL). */
 int  gpmood_get_state(gpmood_ctx* ctx, double* u_host, double* t, int* niter);
+/* The same two calls with a device array (padded layout) in place of the host one. */
+int  gpmood_set_state_dev(gpmood_ctx* ctx, const double* d_u, double t);
+int  gpmood_get_state_dev(gpmood_ctx* ctx, double* d_u);
 /* CellGPO(1:lf,1:nf) after the last stage ("ordr" of output.f90:128), x fastest. */
 int  gpmood_get_orders(gpmood_ctx* ctx, signed char* orders);
 /* The main.f90 loop: up to nsteps steps of Setdt + time_stepping + t += dt,
@@ -249,6 +252,32 @@ int  gpmood_nn_loss_grad(const float* d_params, const float* d_x, const float* d
 /* One bias-corrected Adam step (step counts from 1). */
 int  gpmood_nn_adam(float* d_params, const float* d_grad, float* d_m, float* d_v, int step,
                     float lr, float beta1, float beta2, float eps, void* stream);
+
+/* ---- adjoint of the step with frozen MOOD order masks ----
+ *
+ * No reference counterpart: gp-mood-code has no adjoint.  A recording holds,
+ * for nsteps steps taken by gpmood_advance, every step's t and dt and the
+ * padded CellGPO of its three RK stages (the frozen masks), plus a copy of the
+ * state every `every` steps.  With masks and dt frozen a step is a smooth map
+ * of the interior state; gpmood_adj_backward applies the transpose of its
+ * Jacobian along the recorded trajectory, recomputing each segment of `every`
+ * steps from its checkpoint.  Boundary types: Neumann, periodic, reflective.
+ * Device arrays use the state's padded layout; ghost entries of the returned
+ * adjoint are zero (stage 1 overwrites the input's ghosts).  The context must
+ * outlive the recording; recording and replay leave its state untouched
+ * except that recording advances it by nsteps. */
+typedef struct gpmood_adjoint gpmood_adjoint;
+int  gpmood_adj_record(gpmood_ctx* ctx, int nsteps, int every, gpmood_adjoint** out);
+void gpmood_adj_destroy(gpmood_adjoint* a);
+/* Steps recorded (fewer than asked if tmax was reached) and their t and dt
+ * (arrays of at least that many doubles, or NULL). */
+int  gpmood_adj_info(const gpmood_adjoint* a, int* nsteps, double* t, double* dt);
+/* Padded CellGPO (ncell bytes) of RK stage `stage` of step `step`. */
+int  gpmood_adj_orders(const gpmood_adjoint* a, int step, int stage, signed char* orders_host);
+/* d_uN = the recorded steps applied to d_u0 with the frozen masks and dt. */
+int  gpmood_adj_replay(gpmood_adjoint* a, const double* d_u0, double* d_uN);
+/* d_lam0 = (d u_N / d u_0)^T d_lamN along the recorded trajectory. */
+int  gpmood_adj_backward(gpmood_adjoint* a, const double* d_lamN, double* d_lam0);
 
 #ifdef __cplusplus
 }
