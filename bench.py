@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--fp-mode", choices=("fast", "exact"), default="fast")
     ap.add_argument("--e2e-steps", type=int, default=5)
     ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--nn", type=int, default=1, help="also time the NN-gated variant (0: skip)")
+    ap.add_argument("--batch-problems", type=int, default=1024)
+    ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batched form (0: skip)")
+    ap.add_argument("--adjoint", type=int, default=1, help="also time the adjoint form (0: skip)")
     return ap.parse_args()
 
 
@@ -161,6 +165,127 @@ def cpu_oracle_rate(n, steps, threads):
     _, k = st.run(U, 0.0, steps)
     el = time.perf_counter() - t0
     return n * n * k / el, k, el
+
+
+GATE = ROOT / "gp-mood_gb300" / "gates" / "gate_sedov_rp2d3.txt"
+
+
+def _rel_l1(a, b):
+    import numpy as np
+    I = (slice(4, -4), slice(4, -4))
+    return [float(np.abs(a[I + (k,)] - b[I + (k,)]).sum() / np.abs(b[I + (k,)]).sum()) for k in range(4)]
+
+
+def measure_nn_gated(pkg, n, K, W, fp, U0, plain_final, plain_ms, diag_steps=5):
+    """The same K timed steps with the MLP gate (method NN_GP_MOOD), the gate's
+    flags against plain MOOD's stage-1 decisions, and the state difference."""
+    import numpy as np
+    import torch
+    from gpmood_gb300 import nn_train as T
+    if not GATE.exists():
+        return {"unavailable": f"no trained gate parameters ({GATE.name})"}
+    params = T.load_text(str(GATE))
+    meta_f = GATE.with_suffix(".json")
+    thr = float(json.loads(meta_f.read_text()).get("threshold", 0.0)) if meta_f.exists() else 0.0
+    with pkg.Solver(lf=n, nf=n, bc_type=pkg.REFLECTIVE, tmax=TMAX, fp_mode=fp, method=pkg.NN_GP_MOOD) as s:
+        s.set_nn(params)
+        s.set_nn_threshold(thr)
+        s.set_state(U0, 0.0)
+        s.advance(W)
+        det0 = s.counters().detected_total
+        stream = torch.cuda.ExternalStream(s.stream)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        done = s.advance(K)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        det = s.counters().detected_total - det0
+        Ug, tg, _ = s.get_state()
+    Up, tp = plain_final
+    # gate decisions against plain MOOD on the plain trajectory (untimed)
+    missed = extra = hits = 0
+    with pkg.Solver(lf=n, nf=n, bc_type=pkg.REFLECTIVE, tmax=TMAX, fp_mode=fp) as s:
+        s.set_nn(params)
+        s.set_nn_threshold(thr)
+        s.set_state(Up, tp)
+        for _ in range(diag_steps):
+            gated, _ = s.nn_predict()
+            s.advance(1)
+            low = s.stage_orders(0) < 5
+            g = gated.astype(bool)
+            hits += int((g & low).sum())
+            missed += int((~g & low).sum())
+            extra += int((g & ~low).sum())
+    return {"value": n * n * done / (ms * 1e-3), "unit": "cell-updates/s", "ms_per_step": ms / max(done, 1),
+            "speedup_vs_plain": plain_ms / (ms / max(done, 1)), "steps": done,
+            "rel_l1_vs_plain_after_steps": _rel_l1(Ug, Up), "t_gated": tg, "t_plain": tp,
+            "a_posteriori_detections_timed_steps": det, "logit_threshold": thr,
+            "gate_vs_plain_stage1": {"steps": diag_steps, "hits": hits, "missed": missed, "extra": extra},
+            "gate": GATE.name}
+
+
+def measure_batched(pkg, nprob, steps, fp):
+    """The batched form: nprob seeded four-quadrant Riemann problems of sizes
+    {64,96,128,192,256}^2 stepped together (persistent kernels, CUDA graphs)."""
+    import numpy as np
+    import torch
+    from gpmood_gb300 import ic
+    sizes, states = [], []
+    for i in range(nprob):
+        U, m = ic.random_riemann(i)
+        # Boundary_C with BC_type 17 (Neumann): ghosts copy the edge cells
+        states.append(np.ascontiguousarray(np.pad(U[4:-4, 4:-4], ((4, 4), (4, 4), (0, 0)), mode="edge")))
+        sizes.append((m, m))
+    with pkg.Batch(sizes, lf=64, nf=64, bc_type=pkg.NEUMANN, tmax=1e30, fp_mode=fp) as b:
+        for i, U in enumerate(states):
+            b.set_state(i, U, 0.0)
+        tile, tile_ms = b.autotune()
+        b.advance(3)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        b.advance(steps)
+        torch.cuda.synchronize()
+        el = time.perf_counter() - t0
+        st = b.stats()
+    cells = st["interior_cells"]
+    return {"workload": f"{nprob} seeded 4-quadrant Riemann problems (PCG64 seed = index; rho~U[0.1,2], "
+                        f"p~U[0.02,2], u,v~U[-1.5,1.5], split~U[0.3,0.8]^2, size~U{{64,96,128,192,256}}^2), "
+                        f"Neumann BCs, per-problem dt",
+            "value": cells * steps / el, "unit": "cell-updates/s", "ms_per_step": 1e3 * el / steps,
+            "timed_steps": steps, "warmup": 3, "interior_cells": cells, "graphed": st["graphed"],
+            "tile": int(tile), "tile_flux_ms": [float(x) for x in tile_ms], "status": st["status"],
+            "timing": "host clock around gpmood_batch_advance (synchronous) with device sync on both sides"}
+
+
+def measure_adjoint(pkg):
+    """The adjoint form: 50 recorded steps of the 128^2 periodic vortex and
+    the checkpointed backward (every 10 steps)."""
+    import torch
+    from gpmood_gb300 import ic
+    n, nsteps, every = 128, 50, 10
+    with pkg.Solver(lf=n, nf=n, lx=10.0, ly=10.0, bc_type=pkg.PERIODIC, tmax=1e30, fp_mode=pkg.FP_EXACT) as s:
+        U = ic.isentropic_vortex(n, n, 10.0, 10.0, beta=5.0)
+        s.Boundary_C(U, 0.0)
+        s.set_state(U, 0.0)
+        t0 = time.perf_counter()
+        rec = s.adj_record(nsteps, every)
+        t_rec = time.perf_counter() - t0
+        lam = torch.zeros(s.shape, dtype=torch.float64, device="cuda")
+        lam[4:-4, 4:-4, 0] = 1.0
+        out = torch.empty_like(lam)
+        rec.backward(lam.data_ptr(), out.data_ptr())  # warm-up
+        t0 = time.perf_counter()
+        rec.backward(lam.data_ptr(), out.data_ptr())
+        t_bwd = time.perf_counter() - t0
+        rec.close()
+    return {"workload": "isentropic vortex beta=5, 128^2 periodic on [0,10]^2, 50 SSP-RK3 steps, J=sum rho^2 dxdy, "
+                        "checkpoints every 10 steps",
+            "forward_ms_per_step": 1e3 * t_rec / nsteps, "backward_ms_per_step": 1e3 * t_bwd / nsteps,
+            "backward_over_forward": t_bwd / t_rec,
+            "timing": "host clock around synchronous C-ABI calls (record = gpmood_advance with mask capture; "
+                      "backward includes the segment recomputation)"}
 
 
 def run_reference(args, ws, rank):
@@ -292,6 +417,14 @@ def run_ours(args, ws, rank, local):
                     "peak_source": "MEASURED_PEAKS.json hbm_gbs" if peaks else "fallback 6.8 TB/s",
                     "note": "whole step, 256 algorithmic bytes per cell-update; the path is FP64-pipe bound"}
 
+    forms = {}
+    if args.nn:
+        forms["nn_gated"] = measure_nn_gated(pkg, n, K, W, fp, U0, (Uend, t_end), el_ms / max(done, 1))
+    if args.batch_steps > 0:
+        forms["batched"] = measure_batched(pkg, args.batch_problems, args.batch_steps, fp)
+    if args.adjoint:
+        forms["adjoint"] = measure_adjoint(pkg)
+
     cpu = None
     if rank == 0 and ws == 1 and args.cpu_steps > 0:
         threads = os.cpu_count() or 1
@@ -313,6 +446,8 @@ def run_ours(args, ws, rank, local):
         "fp64_peak_gflops": peak_fp64_gflops,
         "flops_per_cell_update": FLOPS_PER_CELL_UPDATE,
         "achieved_step_tflops": FLOPS_PER_CELL_UPDATE * value / ws / 1e12,
+        "mood_share_of_step": tm.mood_ms / el_ms if el_ms else None,
+        "forms": forms,
     }
     if rank == 0:
         print(json.dumps(line), flush=True)

@@ -213,5 +213,25 @@ extern "C" int gpm_gp_presim(double ell_o_dx, double lx, double ly, int lf, int 
             }
         }
     }
+    if (ngp == 3) {  // mirror-symmetric split of zt for the fast kernels
+        for (int o = 0; o < 3; o++) {
+            const int na = o == 2 ? 5 : (o == 1 ? 3 : 1), npair = o == 2 ? 4 : (o == 1 ? 1 : 0);
+            for (int face = 0; face < 4; face++) {
+                const int dir = (face == 0 || face == 2) ? 0 : 1;
+                const double (*z)[13] = out->zt[o][face];
+                GpSym& sy = out->sym[o][face];
+                for (int k = 0; k < na; k++) {
+                    sy.a0[k] = z[0][gpm_sym_axis(dir, k)];
+                    sy.a1[k] = z[1][gpm_sym_axis(dir, k)];
+                }
+                for (int k = 0; k < npair; k++) {
+                    const int m = gpm_sym_pair(dir, k, 0), mm = gpm_sym_pair(dir, k, 1);
+                    sy.al[k] = 0.5 * (z[0][m] + z[0][mm]);
+                    sy.be[k] = 0.5 * (z[0][m] - z[0][mm]);
+                    sy.ga[k] = z[1][m];
+                }
+            }
+        }
+    }
     return 0;
 }

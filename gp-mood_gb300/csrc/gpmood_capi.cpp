@@ -733,37 +733,27 @@ struct gpmood_adjoint {
     double* dCk;                 // nck checkpoints (U_{k*every})
     double* dSeg;                // 3*every+1 stage inputs of one segment
     double *dLam, *dLamB, *dTA, *dAcc, *dTmp, *dMu, *dFace;
-    DevScalars* dSc;             // the adjoint's own t, dt, qx, qy
-    DevScalars* hSc;             // pinned mirror
+    DevScalars* dStepSc;         // per step: t, dt, dt/dx, dt/dy of the recording
 };
 
 namespace {
 
 double* adj_state(gpmood_adjoint* a, double* base, int i) { return base + (size_t)i * a->c->ncell * 4; }
 
-int adj_set_time(gpmood_adjoint* a, int step) {
-    gpmood_ctx* c = a->c;
-    a->hSc->t = a->t[step];
-    a->hSc->dt = a->dt[step];
-    a->hSc->qx = a->dt[step] / c->g.dx;
-    a->hSc->qy = a->dt[step] / c->g.dy;
-    CU(cudaMemcpyAsync(a->dSc, a->hSc, 4 * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-    return 0;
-}
-
 // One Forward_Euler stage at frozen orders: Boundary_C(uin), fluxes at
 // min(CellGPO) per face, flux-difference update without DETECTION, Boundary_C(uout).
-void adj_frozen_stage(gpmood_adjoint* a, double* uin, double* uout, const int8_t* ord, int stage) {
+void adj_frozen_stage(gpmood_adjoint* a, int step, double* uin, double* uout, const int8_t* ord, int stage) {
     gpmood_ctx* c = a->c;
     const KernelTable& kt = *c->kt;
+    DevScalars* sc = a->dStepSc + step;
     StageArgs sa = stage_args(c, uin, uout, stage, false);
     sa.g.method = GPMOOD_GP_SE;  // no DETECTION
     sa.order = const_cast<int8_t*>(ord);
-    sa.sc = a->dSc;
-    kt.bc(c->g, uin, a->dSc, stage, c->stream);
+    sa.sc = sc;
+    kt.bc(c->g, uin, sc, stage, c->stream);
     kt.flux_all(sa, c->w, c->stream);
     kt.update_detect(sa, c->w, 0, c->stream);
-    kt.bc(c->g, uout, a->dSc, stage, c->stream);
+    kt.bc(c->g, uout, sc, stage, c->stream);
 }
 
 const int8_t* adj_ord(const gpmood_adjoint* a, int step, int stage) {
@@ -774,13 +764,11 @@ const int8_t* adj_ord(const gpmood_adjoint* a, int step, int stage) {
 // the stage inputs X1, X2 in x1, x2.
 int adj_replay_step(gpmood_adjoint* a, int step, double* x0, double* x1, double* x2, double* next) {
     gpmood_ctx* c = a->c;
-    int rc = adj_set_time(a, step);
-    if (rc) return rc;
-    adj_frozen_stage(a, x0, x1, adj_ord(a, step, 0), 0);
-    adj_frozen_stage(a, x1, x2, adj_ord(a, step, 1), 1);
-    c->kt->combine(c->g, x0, x2, 0.75, 0.25, 0, a->dSc, c->stream);
-    adj_frozen_stage(a, x2, next, adj_ord(a, step, 2), 2);
-    c->kt->combine(c->g, x0, next, 1. / 3, 2. / 3, 0, a->dSc, c->stream);
+    adj_frozen_stage(a, step, x0, x1, adj_ord(a, step, 0), 0);
+    adj_frozen_stage(a, step, x1, x2, adj_ord(a, step, 1), 1);
+    c->kt->combine(c->g, x0, x2, 0.75, 0.25, 0, a->dStepSc, c->stream);
+    adj_frozen_stage(a, step, x2, next, adj_ord(a, step, 2), 2);
+    c->kt->combine(c->g, x0, next, 1. / 3, 2. / 3, 0, a->dStepSc, c->stream);
     return check_launch(c, "adjoint replay");
 }
 
@@ -807,8 +795,7 @@ void adj_free(gpmood_adjoint* a) {
     delete[] a->dt;
     cudaFree(a->dOrd); cudaFree(a->dCk); cudaFree(a->dSeg);
     cudaFree(a->dLam); cudaFree(a->dLamB); cudaFree(a->dTA); cudaFree(a->dAcc); cudaFree(a->dTmp);
-    cudaFree(a->dMu); cudaFree(a->dFace); cudaFree(a->dSc);
-    if (a->hSc) cudaFreeHost(a->hSc);
+    cudaFree(a->dMu); cudaFree(a->dFace); cudaFree(a->dStepSc);
     delete a;
 }
 
@@ -843,16 +830,13 @@ int gpmood_adj_record(gpmood_ctx* c, int nsteps, int every, gpmood_adjoint** out
     AALLOC(a->dTmp, sb);
     AALLOC(a->dMu, sb);
     AALLOC(a->dFace, 2 * c->ncell * 8 * GPM_MAXGP * sizeof(double));
-    AALLOC(a->dSc, sizeof(DevScalars));
+    AALLOC(a->dStepSc, (size_t)nsteps * sizeof(DevScalars));
 #undef AALLOC
-    ok = ok && cudaMallocHost((void**)&a->hSc, sizeof(DevScalars)) == cudaSuccess;
     if (ok) {  // adjoint buffers keep zero ghosts for their whole life
         cudaStream_t s = c->stream;
         ok = cudaMemsetAsync(a->dLam, 0, sb, s) == cudaSuccess && cudaMemsetAsync(a->dLamB, 0, sb, s) == cudaSuccess &&
              cudaMemsetAsync(a->dTA, 0, sb, s) == cudaSuccess && cudaMemsetAsync(a->dAcc, 0, sb, s) == cudaSuccess &&
-             cudaMemsetAsync(a->dTmp, 0, sb, s) == cudaSuccess && cudaMemsetAsync(a->dSc, 0, sizeof(DevScalars), s) == cudaSuccess &&
-             cudaStreamSynchronize(s) == cudaSuccess;
-        if (ok) memset(a->hSc, 0, sizeof(DevScalars));
+             cudaMemsetAsync(a->dTmp, 0, sb, s) == cudaSuccess && cudaStreamSynchronize(s) == cudaSuccess;
     }
     if (!ok) {
         adj_free(a);
@@ -877,6 +861,18 @@ int gpmood_adj_record(gpmood_ctx* c, int nsteps, int every, gpmood_adjoint** out
     }
     if (cudaStreamSynchronize(c->stream) != cudaSuccess) { adj_free(a); return fail(c, GPMOOD_E_CUDA, "adjoint record sync"); }
     if (done == 0) { adj_free(a); return fail(c, GPMOOD_E_STATE, "adjoint: no step taken (t >= tmax)"); }
+    // per-step scalars on the device, so that replays never wait on the host
+    DevScalars* hs = new (std::nothrow) DevScalars[done]();
+    if (!hs) { adj_free(a); return fail(c, GPMOOD_E_ARG, "out of host memory"); }
+    for (int s = 0; s < done; s++) {
+        hs[s].t = a->t[s];
+        hs[s].dt = a->dt[s];
+        hs[s].qx = a->dt[s] / c->g.dx;  // the division of k_dt_finalize
+        hs[s].qy = a->dt[s] / c->g.dy;
+    }
+    const cudaError_t es = cudaMemcpy(a->dStepSc, hs, (size_t)done * sizeof(DevScalars), cudaMemcpyHostToDevice);
+    delete[] hs;
+    if (es != cudaSuccess) { adj_free(a); return fail(c, GPMOOD_E_CUDA, "adjoint scalars: %s", cudaGetErrorString(es)); }
     a->nsteps = done;
     a->nck = (done + every - 1) / every;
     *out = a;
@@ -946,18 +942,18 @@ int gpmood_adj_backward(gpmood_adjoint* a, const double* d_lamN, double* d_lam0)
             const double *x0 = adj_state(a, a->dSeg, i), *x1 = adj_state(a, a->dSeg, i + 1);
             const double* x2 = adj_state(a, a->dSeg, i + 2);
             CU(cudaMemcpyAsync(a->dTA, a->dLam, sb, cudaMemcpyDeviceToDevice, st));
-            kt.combine(c->g, a->dLam, a->dTA, 0.0, 2. / 3, 0, a->dSc, st);      // TA = 2/3 l
+            kt.combine(c->g, a->dLam, a->dTA, 0.0, 2. / 3, 0, a->dStepSc, st);      // TA = 2/3 l
             int rc = adj_stage_vjp(a, s, 2, x2, a->dTA, a->dLamB);             // l2
             if (rc) return rc;
             CU(cudaMemcpyAsync(a->dAcc, a->dLam, sb, cudaMemcpyDeviceToDevice, st));
-            kt.combine(c->g, a->dLamB, a->dAcc, 0.75, 1. / 3, 0, a->dSc, st);  // acc = 1/3 l + 3/4 l2
+            kt.combine(c->g, a->dLamB, a->dAcc, 0.75, 1. / 3, 0, a->dStepSc, st);  // acc = 1/3 l + 3/4 l2
             CU(cudaMemcpyAsync(a->dTA, a->dLamB, sb, cudaMemcpyDeviceToDevice, st));
-            kt.combine(c->g, a->dLamB, a->dTA, 0.0, 0.25, 0, a->dSc, st);     // TA = 1/4 l2
+            kt.combine(c->g, a->dLamB, a->dTA, 0.0, 0.25, 0, a->dStepSc, st);     // TA = 1/4 l2
             rc = adj_stage_vjp(a, s, 1, x1, a->dTA, a->dLamB);                 // l1
             if (rc) return rc;
             rc = adj_stage_vjp(a, s, 0, x0, a->dLamB, a->dTmp);                // S0^T(l1)
             if (rc) return rc;
-            kt.combine(c->g, a->dAcc, a->dTmp, 1.0, 1.0, 0, a->dSc, st);      // l_s = acc + S0^T(l1)
+            kt.combine(c->g, a->dAcc, a->dTmp, 1.0, 1.0, 0, a->dStepSc, st);      // l_s = acc + S0^T(l1)
             double* tmp = a->dLam;
             a->dLam = a->dTmp;
             a->dTmp = tmp;

@@ -92,6 +92,43 @@ __device__ __forceinline__ void gp_recon(const double* __restrict__ zface, const
     }
 }
 
+#if !GPM_EXACT
+__device__ __forceinline__ double cell_var(const Cell& c, int k) {
+    return k == 0 ? c.r : (k == 1 ? c.mx : (k == 2 ? c.my : c.e));
+}
+
+// The three Gauss-point states of one face from the mirror-symmetric split
+// (GpSym): same values as gp_recon<NP, 3> up to rounding, 32 instead of 39
+// FP64 operations per variable at NP = 13.
+template <int DIR, int NP>
+__device__ __forceinline__ void gp_recon_sym3(const GpSym& c, const Cell* q, double (*u)[4]) {
+    constexpr int NA = NP == 13 ? 5 : 3, NPR = NP == 13 ? 4 : 1;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        double a0 = c.a0[0] * cell_var(q[gpm_sym_axis(DIR, 0)], k);
+        double a1 = c.a1[0] * cell_var(q[gpm_sym_axis(DIR, 0)], k);
+#pragma unroll
+        for (int i = 1; i < NA; i++) {
+            const double v = cell_var(q[gpm_sym_axis(DIR, i)], k);
+            a0 = a0 + c.a0[i] * v;
+            a1 = a1 + c.a1[i] * v;
+        }
+        double b = 0.0;
+#pragma unroll
+        for (int i = 0; i < NPR; i++) {
+            const double qm = cell_var(q[gpm_sym_pair(DIR, i, 0)], k), qmm = cell_var(q[gpm_sym_pair(DIR, i, 1)], k);
+            const double S = qm + qmm, D = qm - qmm;
+            a0 = a0 + c.al[i] * S;
+            a1 = a1 + c.ga[i] * S;
+            b = (i == 0) ? c.be[0] * D : b + c.be[i] * D;
+        }
+        u[0][k] = a0 + b;
+        u[1][k] = a1;
+        u[2][k] = a0 - b;
+    }
+}
+#endif
+
 // Primitive recovery of one face state, c2p_local (physics.f90:51-75): normal
 // velocity vn, tangential velocity vt, vn^2, pressure, sound speed, admissibility.
 struct Prim {
@@ -104,7 +141,7 @@ struct Prim {
 };
 
 template <int DIR>
-__device__ __forceinline__ Prim c2p(const double* u) {
+__device__ __forceinline__ Prim c2p(const double* u, double ir_in = 0.0) {
     Prim s;
 #if GPM_EXACT
     const double vx = u[1] / u[0];
@@ -112,7 +149,7 @@ __device__ __forceinline__ Prim c2p(const double* u) {
     s.p = (GPM_GAMMA - 1.) * (u[3] - (0.5 * (u[1] * u[1] + u[2] * u[2]) / u[0]));
     s.c = sqrt(GPM_GAMMA * s.p / u[0]);
 #else
-    const double ir = 1.0 / u[0];
+    const double ir = ir_in;  // 1/rho, supplied by the caller
     const double vx = u[1] * ir;
     const double vy = u[2] * ir;
     s.p = (GPM_GAMMA - 1.) * (u[3] - 0.5 * (u[1] * vx + u[2] * vy));
@@ -148,8 +185,14 @@ __device__ __forceinline__ void phys_flux(const double* u, const Prim& s, double
 // skipped quantity is unused by that branch, so the result is unchanged.
 template <int DIR>
 __device__ __forceinline__ void hllc(const double* ul, const double* ur, double* F) {
+#if GPM_EXACT
     const Prim L = c2p<DIR>(ul);
     const Prim R = c2p<DIR>(ur);
+#else
+    const double rr = 1.0 / (ul[0] * ur[0]);  // one division for both 1/rho
+    const Prim L = c2p<DIR>(ul, ur[0] * rr);
+    const Prim R = c2p<DIR>(ur, ul[0] * rr);
+#endif
     const double SL = fmin(L.vn - L.c, R.vn - R.c);
     const double SR = fmax(L.vn + L.c, R.vn + R.c);
     if (!(L.adm && R.adm)) {  // :166

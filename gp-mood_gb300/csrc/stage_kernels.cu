@@ -137,6 +137,19 @@ void launch_bc(const GridGeom& g, double* u, const DevScalars* sc, int stage, cu
 // reconstructs the two face states at every Gauss point (13-point GP dot
 // products), solves HLLC and integrates along the face.
 
+// Gauss-point states of face `face` of one cell at order index o: the fast
+// kernels use the mirror-symmetric split for ngp = 3 above first order.
+template <int DIR, int NP, int NGP>
+__device__ __forceinline__ void recon_face(const GpWeights& w, int o, int face, const Cell* q, double (*u)[4]) {
+#if !GPM_EXACT
+    if constexpr (NGP == 3 && NP > 1) {
+        gp_recon_sym3<DIR, NP>(w.sym[o][face], q, u);
+        return;
+    }
+#endif
+    gp_recon<NP, NGP>(&w.zt[o][face][0][0], q, u);
+}
+
 template <int DIR, int NP, int NGP>
 __device__ __forceinline__ void face_from_tile(const GpWeights& w, int o, const Cell (*tile)[HX], int tx, int ty,
                                                double* F) {
@@ -147,14 +160,14 @@ __device__ __forceinline__ void face_from_tile(const GpWeights& w, int o, const 
         Cell q[NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) q[m] = tile[ty + st_oy(m)][tx + st_ox(m)];
-        gp_recon<NP, NGP>(&w.zt[o][FL][0][0], q, uL);
+        recon_face<DIR, NP, NGP>(w, o, FL, q, uL);
     }
     {
         constexpr int hx = DIR == 0 ? 1 : 0, hy = DIR == 0 ? 0 : 1;
         Cell q[NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) q[m] = tile[ty + hy + st_oy(m)][tx + hx + st_ox(m)];
-        gp_recon<NP, NGP>(&w.zt[o][FH][0][0], q, uR);
+        recon_face<DIR, NP, NGP>(w, o, FH, q, uR);
     }
     quad_flux<DIR, NGP>(uL, uR, w.gw, F);
 }
@@ -303,13 +316,13 @@ __device__ __forceinline__ void face_global(const GridGeom& g, const GpWeights& 
         Cell q[NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) q[m] = ld_cell(uin + 4 * (c0 + st_ox(m) + row * st_oy(m)));
-        gp_recon<NP, NGP>(&w.zt[o][FL][0][0], q, uL);
+        recon_face<DIR, NP, NGP>(w, o, FL, q, uL);
     }
     {
         Cell q[NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) q[m] = ld_cell(uin + 4 * (c1 + st_ox(m) + row * st_oy(m)));
-        gp_recon<NP, NGP>(&w.zt[o][FH][0][0], q, uR);
+        recon_face<DIR, NP, NGP>(w, o, FH, q, uR);
     }
     quad_flux<DIR, NGP>(uL, uR, w.gw, F);
 }
@@ -701,14 +714,14 @@ __device__ __forceinline__ void face_tile_b(const GpWeights& w, int o, const Cel
         Cell q[NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) q[m] = tile[(ty + st_oy(m)) * HXB + tx + st_ox(m)];
-        gp_recon<NP, NGP>(&w.zt[o][FL][0][0], q, uL);
+        recon_face<DIR, NP, NGP>(w, o, FL, q, uL);
     }
     {
         constexpr int hx = DIR == 0 ? 1 : 0, hy = DIR == 0 ? 0 : 1;
         Cell q[NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) q[m] = tile[(ty + hy + st_oy(m)) * HXB + tx + hx + st_ox(m)];
-        gp_recon<NP, NGP>(&w.zt[o][FH][0][0], q, uR);
+        recon_face<DIR, NP, NGP>(w, o, FH, q, uR);
     }
     quad_flux<DIR, NGP>(uL, uR, w.gw, F);
 }
