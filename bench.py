@@ -56,6 +56,8 @@ def parse():
     ap.add_argument("--batch-problems", type=int, default=1024)
     ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batched form (0: skip)")
     ap.add_argument("--adjoint", type=int, default=1, help="also time the adjoint form (0: skip)")
+    ap.add_argument("--final", action="store_true",
+                    help="run plain and NN-gated GP-MOOD from t=0 to t_final=0.05 and compare them")
     return ap.parse_args()
 
 
@@ -71,6 +73,30 @@ def dist_setup(args):
             torch.cuda.set_device(local)
         dist.init_process_group(backend=backend)
     return ws, rank, local
+
+
+def dist_barrier(ws: int) -> None:
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def dist_max(x: float, ws: int) -> float:
+    """Max of a host scalar over the ranks (NCCL: through a device tensor)."""
+    if ws == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_value(cells_per_rank: int, steps: int, elapsed_ms: float, ws: int) -> float:
+    """Whole-job throughput of ws independent replicas: the cell-updates of all
+    ranks over the slowest rank's time."""
+    return ws * cells_per_rank * steps / (dist_max(elapsed_ms, ws) * 1e-3)
 
 
 def workload_name(n):
@@ -288,6 +314,54 @@ def measure_adjoint(pkg):
                       "backward includes the segment recomputation)"}
 
 
+def run_final(args):
+    """Plain and NN-gated GP-MOOD on the Sedov problem from t=0 to t_final:
+    time to solution, steps, and the relative L1 difference of the final states."""
+    import numpy as np
+    import torch
+    import __graft_entry__ as ge
+    pkg = ge.import_package()
+    from gpmood_gb300 import ic, nn_train as T
+    n = args.n
+    fp = pkg.FP_FAST if args.fp_mode == "fast" else pkg.FP_EXACT
+    U0 = ic.sedov(n, n)
+    params = T.load_text(str(GATE))
+    meta_f = GATE.with_suffix(".json")
+    thr = float(json.loads(meta_f.read_text()).get("threshold", 0.0)) if meta_f.exists() else 0.0
+    out = {}
+    finals = {}
+    for name, method in (("plain", pkg.GP_MOOD), ("nn_gated", pkg.NN_GP_MOOD)):
+        with pkg.Solver(lf=n, nf=n, bc_type=pkg.REFLECTIVE, tmax=TMAX, fp_mode=fp, method=method) as s:
+            s.Boundary_C(U0, 0.0)
+            if method == pkg.NN_GP_MOOD:
+                s.set_nn(params)
+                s.set_nn_threshold(thr)
+            s.set_state(U0, 0.0)
+            s.set_timing(True)
+            stream = torch.cuda.ExternalStream(s.stream)
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            torch.cuda.synchronize()
+            ev0.record(stream)
+            steps = s.advance(1 << 30)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+            ms = ev0.elapsed_time(ev1)
+            U, t, _ = s.get_state()
+            c = s.counters()
+            tm = s.timing()
+        finals[name] = U
+        out[name] = {"steps": steps, "t": t, "seconds": ms / 1e3, "value": n * n * steps / (ms * 1e-3),
+                     "unit": "cell-updates/s", "detected_total": c.detected_total,
+                     "max_passes_stage": c.max_passes_stage, "status_flags": c.status_flags,
+                     "mood_share": tm.mood_ms / ms if ms else None}
+    out["nn_gated"]["speedup_vs_plain"] = out["plain"]["seconds"] / out["nn_gated"]["seconds"]
+    out["rel_l1_final"] = _rel_l1(finals["nn_gated"], finals["plain"])
+    line = {"metric": "time to t_final", "workload": workload_name(n) + f", t_final={TMAX}",
+            "fp_mode": args.fp_mode, "gate": GATE.name, "logit_threshold": thr, **out}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
@@ -330,17 +404,10 @@ def run_ours(args, ws, rank, local):
     peak_fp64_gflops = probe_fp64()
 
     def barrier():
-        if ws > 1:
-            import torch.distributed as dist
-            dist.barrier()
+        dist_barrier(ws)
 
     def max_over_ranks(x: float) -> float:
-        if ws == 1:
-            return x
-        import torch.distributed as dist
-        t = torch.tensor([x], dtype=torch.float64, device="cuda")
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        return float(t.item())
+        return dist_max(x, ws)
 
     # ---- device-resident throughput (inputs in HBM) ----
     solver.set_state(U0, 0.0)
@@ -359,14 +426,15 @@ def run_ours(args, ws, rank, local):
     torch.cuda.synchronize()
     barrier()
     clk = clocks.stop()
-    el_ms = max_over_ranks(ev0.elapsed_time(ev1))
+    el_local = ev0.elapsed_time(ev1)
+    value = replica_value(n * n, done, el_local, ws)
+    el_ms = max_over_ranks(el_local)
     tm = solver.timing()
     ctr = solver.counters()
     Uend, t_end, _ = solver.get_state()
     checksum = {"t": t_end, "sum_rho": float(Uend[4:-4, 4:-4, 0].sum()),
                 "sum_E": float(Uend[4:-4, 4:-4, 3].sum())}
     launches = ctr.kernel_launches - launches0
-    value = ws * n * n * done / (el_ms * 1e-3)
 
     # ---- end to end through the reference-facing C ABI with host buffers ----
     Uh = torch.empty(U0.shape, dtype=torch.float64).pin_memory()
@@ -457,7 +525,9 @@ def run_ours(args, ws, rank, local):
 def main():
     args = parse()
     ws, rank, local = dist_setup(args)
-    if args.impl == "reference":
+    if args.final:
+        rc = run_final(args) if rank == 0 else 0
+    elif args.impl == "reference":
         rc = run_reference(args, ws, rank)
     else:
         rc = run_ours(args, ws, rank, local)

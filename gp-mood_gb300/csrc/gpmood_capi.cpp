@@ -109,16 +109,26 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* pa
     c->ctr.kernel_launches += 2;
     bool uniform = true;
     CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, s));  // CellGPO = mord, :48
+    CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), s));
     if (c->p.method == GPMOOD_NN_GP_MOOD && c->niter + 1 > c->p.nsteps_with_no_nn) {
-        int rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, s);  // :51-56
+        // gated cells start at mord-2 (:51-56) and are listed in tlist[1]
+        int rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1], s);
         if (rc < 0) return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
         c->ctr.kernel_launches += rc;
         uniform = false;
     }
-    CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), s));
     StageArgs a = stage_args(c, uin, uout, stage, uniform);
     if (c->timing) cudaEventRecord(c->ev[0], s);
-    kt.flux_all(a, c->w, s);
+    // First pass over every face at mord; the faces of gated cells are then
+    // recomputed at min(CellGPO) of their two cells, which gives every stored
+    // flux the value of a first pass at the gated orders.
+    StageArgs au = a;
+    au.uniform_order = 1;
+    kt.flux_all(au, c->w, s);
+    if (!uniform) {
+        kt.mood_faces(a, c->w, 1, c->p.lf * c->p.nf, s);
+        c->ctr.kernel_launches += 1;
+    }
     if (c->timing) cudaEventRecord(c->ev[1], s);
     kt.update_detect(a, c->w, 0, s);
     if (c->timing) cudaEventRecord(c->ev[2], s);
@@ -631,7 +641,9 @@ int gpmood_nn_predict(gpmood_ctx* c, signed char* gated, long long* n_gated) {
     if (!nn_gate_loaded(c->nn)) return fail(c, GPMOOD_E_STATE, "no gate parameters (gpmood_set_nn)");
     CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, c->stream));
     CU(cudaMemsetAsync(&c->dSc->apriori_step, 0, sizeof(unsigned long long), c->stream));
-    if (nn_gate_orders(c->nn, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, c->stream) < 0)
+    CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), c->stream));
+    if (nn_gate_orders(c->nn, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1],
+                       c->stream) < 0)
         return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
     CU(cudaMemcpy2DAsync(gated, (size_t)c->p.lf, c->dOrder + (size_t)GPM_NGC * c->g.nx + GPM_NGC, (size_t)c->g.nx,
                          (size_t)c->p.lf, (size_t)c->p.nf, cudaMemcpyDeviceToHost, c->stream));

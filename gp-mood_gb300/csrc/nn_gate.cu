@@ -168,49 +168,68 @@ __device__ __forceinline__ void warp_forward(const SmemFwd& s, int r0, float b2,
 }
 
 // ---------------------------------------------------------------------------
-// The gate: features of 128 interior cells per CTA, MLP, order update.
+// The gate: a persistent CTA loads the BF16 weights once, then walks tiles of
+// 128 interior cells: features, MLP, order update.  A tile whose cells all
+// have constant stencils (never gated) skips the MLP.
 __global__ void __launch_bounds__(THREADS) k_gate(GridGeom g, const double* __restrict__ u, const float* __restrict__ p,
                                                float thr, int8_t* __restrict__ order,
-                                               unsigned long long* __restrict__ count) {
+                                               unsigned long long* __restrict__ count, int* __restrict__ list,
+                                               int* __restrict__ list_count) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     SmemFwd& s = *reinterpret_cast<SmemFwd*>(smem_raw);
     __shared__ int8_t cst[ROWS];
     __shared__ float logit[ROWS];
     load_weights(s, p);
+    const float b2 = p[P_B2];
     const long long ncells = (long long)g.lf * g.nf;
-    const long long row = (long long)blockIdx.x * ROWS + threadIdx.x;
-    if (threadIdx.x < ROWS) {
-        float x[36];
-        bool c = true;
-        if (row < ncells) {
-            const int l = 1 + (int)(row % g.lf), n = 1 + (int)(row / g.lf);
-            c = cell_features(g, u, l, n, x);
-        } else {
-#pragma unroll
-            for (int k = 0; k < 36; k++) x[k] = 0.f;
-        }
-#pragma unroll
-        for (int k = 0; k < K0; k += 2)
-            *reinterpret_cast<uint32_t*>(&s.x[threadIdx.x][k]) = pack_bf16(k < 36 ? x[k] : 0.f, k + 1 < 36 ? x[k + 1] : 0.f);
-        cst[threadIdx.x] = c ? 1 : 0;
-    }
-    __syncthreads();
+    const long long ntiles = (ncells + ROWS - 1) / ROWS;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    WarpFwd f;
-    warp_forward(s, 16 * warp, p[P_B2], f);
-    if ((lane & 3) == 0) {
-        logit[16 * warp + (lane >> 2)] = f.logit_lo;
-        logit[16 * warp + (lane >> 2) + 8] = f.logit_hi;
+    for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
+        const long long row = tile * ROWS + threadIdx.x;
+        bool c = true;
+        if (threadIdx.x < ROWS) {
+            float x[36];
+            if (row < ncells) {
+                const int l = 1 + (int)(row % g.lf), n = 1 + (int)(row / g.lf);
+                c = cell_features(g, u, l, n, x);
+            } else {
+#pragma unroll
+                for (int k = 0; k < 36; k++) x[k] = 0.f;
+            }
+#pragma unroll
+            for (int k = 0; k < K0; k += 2)
+                *reinterpret_cast<uint32_t*>(&s.x[threadIdx.x][k]) =
+                    pack_bf16(k < 36 ? x[k] : 0.f, k + 1 < 36 ? x[k + 1] : 0.f);
+            cst[threadIdx.x] = c ? 1 : 0;
+        }
+        if (__syncthreads_and(c)) continue;  // every stencil constant: nothing to gate
+        WarpFwd f;
+        warp_forward(s, 16 * warp, b2, f);
+        if ((lane & 3) == 0) {
+            logit[16 * warp + (lane >> 2)] = f.logit_lo;
+            logit[16 * warp + (lane >> 2) + 8] = f.logit_hi;
+        }
+        __syncthreads();
+        bool fire = false;
+        int cidx = 0;
+        if (threadIdx.x < ROWS && row < ncells && !cst[threadIdx.x] && logit[threadIdx.x] > thr) {
+            const int l = 1 + (int)(row % g.lf), n = 1 + (int)(row / g.lf);
+            cidx = (n + 3) * g.nx + (l + 3);
+            order[cidx] = (int8_t)(g.mord - 2);
+            fire = true;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, fire);
+        if (m) {  // warp-aggregated append to the gated-cell list
+            int base = 0;
+            if (lane == 0) {
+                atomicAdd(count, (unsigned long long)__popc(m));
+                base = atomicAdd(list_count, __popc(m));
+            }
+            base = __shfl_sync(0xffffffffu, base, 0);
+            if (fire) list[base + __popc(m & ((1u << lane) - 1))] = cidx;
+        }
+        __syncthreads();  // s.x, cst and logit are rewritten by the next tile
     }
-    __syncthreads();
-    bool fire = false;
-    if (threadIdx.x < ROWS && row < ncells && !cst[threadIdx.x] && logit[threadIdx.x] > thr) {
-        const int l = 1 + (int)(row % g.lf), n = 1 + (int)(row / g.lf);
-        order[(size_t)(n + 3) * g.nx + (size_t)(l + 3)] = (int8_t)(g.mord - 2);
-        fire = true;
-    }
-    const unsigned m = __ballot_sync(0xffffffffu, fire);
-    if (lane == 0 && m) atomicAdd(count, (unsigned long long)__popc(m));
 }
 
 __global__ void k_features(GridGeom g, const double* __restrict__ u, float* __restrict__ x, int8_t* __restrict__ cst) {
@@ -506,17 +525,21 @@ void nn_gate_set_threshold(NnGate* n, float thr) { n->thr = thr; }
 bool nn_gate_loaded(const NnGate* n) { return n && n->loaded; }
 
 int nn_gate_orders(NnGate* n, const GridGeom& g, const double* uin, int8_t* order, unsigned long long* count,
-                   cudaStream_t s) {
+                   int* list, int* list_count, cudaStream_t s) {
     if (!n->loaded || g.mord < 3) return 0;
     const long long cells = (long long)g.lf * g.nf;
-    const int blocks = (int)((cells + ROWS - 1) / ROWS);
+    const long long tiles = (cells + ROWS - 1) / ROWS;
     const size_t sm = sizeof(SmemFwd);
-    static bool attr = false;
-    if (!attr) {
+    static int nsm = 0;
+    if (!nsm) {
+        int dev = 0;
+        cudaGetDevice(&dev);
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+        if (nsm <= 0) nsm = 1;
         cudaFuncSetAttribute(k_gate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        attr = true;
     }
-    k_gate<<<blocks, THREADS, sm, s>>>(g, uin, n->params, n->thr, order, count);
+    const int blocks = (int)(tiles < 4LL * nsm ? tiles : 4LL * nsm);  // persistent: up to 4 CTAs per SM
+    k_gate<<<blocks, THREADS, sm, s>>>(g, uin, n->params, n->thr, order, count, list, list_count);
     return cudaGetLastError() == cudaSuccess ? 1 : -1;
 }
 

@@ -34,9 +34,10 @@ int nn_gate_set(NnGate* n, const float* params, cudaStream_t s);
 void nn_gate_set_threshold(NnGate* n, float logit_threshold);
 bool nn_gate_loaded(const NnGate* n);
 // Overwrite order[] of gated interior cells with mord-2; adds the number of
-// gated cells to *count.  Returns the number of kernels launched, or -1.
+// gated cells to *count and appends their padded indices to list (running
+// length *list_count).  Returns the number of kernels launched, or -1.
 int nn_gate_orders(NnGate* n, const GridGeom& g, const double* uin, int8_t* order, unsigned long long* count,
-                   cudaStream_t s);
+                   int* list, int* list_count, cudaStream_t s);
 
 // Features (FP32, [n][36]) and constant-stencil flags of every interior cell
 // (x fastest), for callers that evaluate or train the network themselves.
