@@ -263,6 +263,16 @@ __device__ __forceinline__ void list_append(bool flag, int* __restrict__ list, i
     if (flag) list[base + __popc(m & ((1u << lane) - 1))] = value;
 }
 
+// Position of the calling thread in an order that deals consecutive work
+// items round-robin over the CTAs (one or a few per SM) and, inside a CTA,
+// over its warps (the SM's sub-partitions).  A short list then spreads over
+// every SM's FP64 units instead of filling the first few CTAs.  Lanes of one
+// warp get items that differ by a multiple of 4 * (number of warps).
+__device__ __forceinline__ int spread_tid() {
+    const int nw = blockDim.x >> 5;
+    return (threadIdx.x & 31) * (gridDim.x * nw) + (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+}
+
 __global__ void __launch_bounds__(256) k_update_detect(StageArgs a, const __grid_constant__ GpWeights w, int cur) {
     const GridGeom& g = a.g;
     const int l = 1 + blockIdx.x * 32 + threadIdx.x, n = 1 + blockIdx.y * 8 + threadIdx.y;
@@ -342,9 +352,9 @@ __device__ __forceinline__ void face_any_order(const StageArgs& a, const GpWeigh
 template <int NGP>
 __global__ void __launch_bounds__(128) k_mood_faces(StageArgs a, const __grid_constant__ GpWeights w, int cur) {
     const int nt = a.sc->ntrb[cur];
-    // 4 faces per troubled cell: x faces (l-1,n), (l,n), y faces (l,n-1), (l,n).
-    // Even work items are x faces, odd ones y faces, so warps stay mostly uniform.
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * nt; i += gridDim.x * blockDim.x) {
+    // 4 faces per troubled cell: x faces (l-1,n), (l,n), y faces (l,n-1), (l,n);
+    // the lanes of a warp get items of one direction (spread_tid).
+    for (int i = spread_tid(); i < 4 * nt; i += gridDim.x * blockDim.x) {
         const size_t c = (size_t)a.tlist[cur][i >> 2];
         const int f = i & 3;
         if ((f & 1) == 0) face_any_order<0, NGP>(a, w, f == 0 ? c - 1 : c);
@@ -363,7 +373,9 @@ __global__ void __launch_bounds__(256) k_mood_cells(StageArgs a, const __grid_co
     // Round the trip count up to a multiple of the stride so whole warps reach
     // list_append together.
     const int lim = ((total + stride - 1) / stride) * stride;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lim; i += stride) {
+    const int st = spread_tid();
+    for (int base = 0; base < lim; base += stride) {
+        const int i = base + st;
         bool trb = false;
         int cval = 0;
         if (i < total) {
@@ -423,6 +435,7 @@ __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_
     const GridGeom& g = a.g;
     const double qx = a.sc->qx, qy = a.sc->qy;
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    const int stid = spread_tid();  // work items are dealt over all SMs
     int cur = 0, pass = 1;  // pass 1 (all faces) ran before this kernel
     for (;;) {
         const int nt = *(volatile int*)&a.sc->ntrb[cur];
@@ -433,7 +446,7 @@ __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_
         }
         pass++;
         // cascade of the troubled cells' orders, mod_subroutine_MOOD.f90:159-163
-        for (int i = gtid; i < nt; i += gstride) {
+        for (int i = stid; i < nt; i += gstride) {
             const int c = a.tlist[cur][i];
             const int o = a.order[c];
             a.order[c] = (int8_t)(o == 3 ? 1 : (o > 3 ? 3 : o));
@@ -444,7 +457,7 @@ __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_
         }
         if (!grid_sync(bar)) return;
         // the four faces of every troubled cell at the new orders
-        for (int i = gtid; i < 4 * nt; i += gstride) {
+        for (int i = stid; i < 4 * nt; i += gstride) {
             const size_t c = (size_t)a.tlist[cur][i >> 2];
             const int f = i & 3;
             if ((f & 1) == 0) face_any_order<0, NGP>(a, w, f == 0 ? c - 1 : c);
@@ -455,7 +468,8 @@ __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_
         const unsigned pid = pass_base + (unsigned)pass;
         const int nxt = cur ^ 1, total = 5 * nt;
         const int lim = ((total + gstride - 1) / gstride) * gstride;
-        for (int i = gtid; i < lim; i += gstride) {
+        for (int base = 0; base < lim; base += gstride) {
+            const int i = base + stid;
             bool trb = false;
             int cval = 0;
             if (i < total) {
@@ -853,7 +867,7 @@ __global__ void kb_mood_mark(BatchArgs a, int cur) {
 template <int NGP>
 __global__ void __launch_bounds__(128) kb_mood_faces(BatchArgs a, int cur) {
     const int nt = a.ntrb[cur];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < 4 * nt; i += gridDim.x * blockDim.x) {
+    for (int i = spread_tid(); i < 4 * nt; i += gridDim.x * blockDim.x) {
         const int2 e = a.tlist[cur][i >> 2];
         const BProb P = a.prob[e.x];
         StageArgs sa;
@@ -878,7 +892,9 @@ __global__ void __launch_bounds__(256) kb_mood_cells(BatchArgs a, int cur) {
     const int total = 5 * nt;
     const int stride = gridDim.x * blockDim.x;
     const int lim = ((total + stride - 1) / stride) * stride;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < lim; i += stride) {
+    const int st = spread_tid();
+    for (int base = 0; base < lim; base += stride) {
+        const int i = base + st;
         bool trb = false;
         int2 val = make_int2(0, 0);
         if (i < total) {
@@ -922,6 +938,7 @@ void blaunch_mood_pass(const BatchArgs& a, int cur, cudaStream_t s) {
 template <int NGP>
 __global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar, int max_pass) {
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
+    const int stid = spread_tid();
     int cur = 0, pass = 1;
     for (;;) {
         const int nt = *(volatile int*)&a.ntrb[cur];
@@ -931,7 +948,7 @@ __global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar
             break;
         }
         pass++;
-        for (int i = gtid; i < nt; i += gstride) {
+        for (int i = stid; i < nt; i += gstride) {
             const int2 e = a.tlist[cur][i];
             int8_t* o = a.order + a.prob[e.x].off + e.y;
             const int v = *o;
@@ -943,7 +960,7 @@ __global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar
             a.ntrb[4] += nt;
         }
         if (!grid_sync(bar)) return;
-        for (int i = gtid; i < 4 * nt; i += gstride) {
+        for (int i = stid; i < 4 * nt; i += gstride) {
             const int2 e = a.tlist[cur][i >> 2];
             const BProb P = a.prob[e.x];
             StageArgs sa;
@@ -962,7 +979,8 @@ __global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar
         const unsigned epoch = (unsigned)*(volatile int*)&a.ntrb[2];
         const int nxt = cur ^ 1, total = 5 * nt;
         const int lim = ((total + gstride - 1) / gstride) * gstride;
-        for (int i = gtid; i < lim; i += gstride) {
+        for (int base = 0; base < lim; base += gstride) {
+            const int i = base + stid;
             bool trb = false;
             int2 val = make_int2(0, 0);
             if (i < total) {
