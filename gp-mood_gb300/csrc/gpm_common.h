@@ -63,7 +63,8 @@ struct DevScalars {
     unsigned long long dtmin_bits;    // Setdt reduction slot (bits of a positive double)
     int ntrb[2];                      // troubled-cell counts, double-buffered lists
     int status;                       // GPMOOD status bits
-    int passes;                       // MOOD passes of the last stage (device loop)
+    int passes_stage[3];              // MOOD passes of each RK stage of the last step (device loop)
+    unsigned stamp_epoch;             // first unused pass stamp of the device MOOD loop
     unsigned long long detected_step; // count_detected_cell of the current step
     unsigned long long apriori_step;
 };
@@ -106,8 +107,9 @@ struct KernelTable {
     void (*cfl)(const GridGeom& g, const double* u, DevScalars* sc, cudaStream_t s);
     void (*dt_finalize)(const GridGeom& g, DevScalars* sc, double dtfinal, cudaStream_t s);
     void (*advance_t)(DevScalars* sc, cudaStream_t s);
-    // MOOD passes 2, 3, ... in one cooperative launch; returns -1 if the launch failed
-    int (*mood_loop)(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, unsigned pass_base,
+    // MOOD passes 2, 3, ... of RK stage `stage` in one cooperative launch; the
+    // pass count goes to sc->passes_stage[stage]; returns -1 if the launch failed
+    int (*mood_loop)(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, int stage,
                      cudaStream_t s);
 };
 

@@ -34,7 +34,6 @@ struct gpmood_ctx {
     GridBar* dBar;                // barrier of the cooperative MOOD loop
     GridBar* hBar;                // pinned mirror
     int* hCount;                  // pinned troubled count
-    unsigned pass_id;
     double t;                     // host mirror of the time
     int niter;
     bool have_state;
@@ -49,7 +48,7 @@ struct gpmood_ctx {
     unsigned hvSeed;
     bool timing;                  // per-kernel CUDA-event timing
     bool trace;                   // GPMOOD_TRACE=1: one line per step on stderr
-    cudaEvent_t ev[4];
+    cudaEvent_t ev[3][4];         // per RK stage: flux, update, MOOD loop boundaries
     gpmood_timing tm;
     char err[512];
 };
@@ -102,9 +101,12 @@ StageArgs stage_args(gpmood_ctx* c, const double* uin, double* uout, int stage, 
 }
 
 // One Forward_Euler stage (mod_FE.f90:20-190) from uin (device) into uout.
-int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* passes) {
+// Nothing here waits for the GPU: pass counts and status come back once per
+// step (run_step).
+int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage) {
     cudaStream_t s = c->stream;
     const KernelTable& kt = *c->kt;
+    cudaEvent_t* ev = c->ev[stage];
     c->kt->bc(c->g, uin, c->dSc, stage, s);  // Boundary_C(Uin), :64
     c->ctr.kernel_launches += 2;
     bool uniform = true;
@@ -118,7 +120,7 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* pa
         uniform = false;
     }
     StageArgs a = stage_args(c, uin, uout, stage, uniform);
-    if (c->timing) cudaEventRecord(c->ev[0], s);
+    if (c->timing) cudaEventRecord(ev[0], s);
     // First pass over every face at mord; the faces of gated cells are then
     // recomputed at min(CellGPO) of their two cells, which gives every stored
     // flux the value of a first pass at the gated orders.
@@ -129,51 +131,22 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* pa
         kt.mood_faces(a, c->w, 1, c->p.lf * c->p.nf, s);
         c->ctr.kernel_launches += 1;
     }
-    if (c->timing) cudaEventRecord(c->ev[1], s);
+    if (c->timing) cudaEventRecord(ev[1], s);
     kt.update_detect(a, c->w, 0, s);
-    if (c->timing) cudaEventRecord(c->ev[2], s);
+    if (c->timing) cudaEventRecord(ev[2], s);
     c->ctr.kernel_launches += 3;
     int rc = check_launch(c, "first MOOD pass");
     if (rc) return rc;
-    if (c->timing) {
-        float ms0 = 0.f, ms1 = 0.f;
-        cudaEventSynchronize(c->ev[2]);
-        cudaEventElapsedTime(&ms0, c->ev[0], c->ev[1]);
-        cudaEventElapsedTime(&ms1, c->ev[1], c->ev[2]);
-        c->tm.flux_ms += ms0;
-        c->tm.flux_launches += 2;
-        c->tm.flux_faces += (long long)(c->p.lf + 1) * c->p.nf + (long long)c->p.lf * (c->p.nf + 1);
-        c->tm.update_ms += ms1;
-        c->tm.update_launches += 1;
-    }
-    long long npass = 1;
     if (c->p.method == GPMOOD_GP_MOOD || c->p.method == GPMOOD_NN_GP_MOOD) {
         // passes 2, 3, ... run on the device in one cooperative launch (the loop
         // of mod_FE.f90:69-174 ends when DETECTION flags no cell)
         const long long cap = c->p.max_mood_iters > 0 ? c->p.max_mood_iters : 2LL * c->p.lf * c->p.nf + 2;
         const int max_pass = cap > 0x7fffffff ? 0x7fffffff : (int)cap;
-        CU(cudaMemsetAsync(c->dBar, 0, sizeof(GridBar), s));
-        if (c->timing) cudaEventRecord(c->ev[0], s);
-        if (kt.mood_loop(a, c->w, c->dBar, max_pass, c->pass_id, s))
+        if (kt.mood_loop(a, c->w, c->dBar, max_pass, stage, s))
             return fail(c, GPMOOD_E_CUDA, "MOOD loop launch: %s", cudaGetErrorString(cudaGetLastError()));
-        if (c->timing) cudaEventRecord(c->ev[3], s);
         c->ctr.kernel_launches += 1;
-        CU(cudaMemcpyAsync(c->hSc, c->dSc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
-        CU(cudaMemcpyAsync(c->hBar, c->dBar, sizeof(GridBar), cudaMemcpyDeviceToHost, s));
-        CU(cudaStreamSynchronize(s));
-        if (c->timing) {
-            float ms = 0.f;
-            cudaEventElapsedTime(&ms, c->ev[0], c->ev[3]);
-            c->tm.mood_ms += ms;
-        }
-        if (c->hBar->err) return fail(c, GPMOOD_E_CUDA, "MOOD loop: grid barrier timed out");
-        npass = c->hSc->passes;
-        c->pass_id += (unsigned)npass;  // stamps of later passes stay unique
-        if (c->hSc->status & GPM_STATUS_MOODCAP) {
-            c->ctr.status_flags |= GPM_STATUS_MOODCAP;
-            return fail(c, GPMOOD_E_MOOD_CAP, "MOOD loop did not converge in %d passes", max_pass);
-        }
     }
+    if (c->timing) cudaEventRecord(ev[3], s);
     CU(cudaMemcpyAsync(c->dStageOrd + (size_t)stage * c->ncell, c->dOrder, c->ncell, cudaMemcpyDeviceToDevice, s));
     if (stage == 0 && c->hvX) {  // training samples of stage 1 (mod_FE.f90:176-181)
         if (nn_harvest(c->g, uin, c->dOrder, c->hvX, c->hvY, c->hvCap, c->hvCount, c->hvKeep,
@@ -183,36 +156,63 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, long long* pa
     }
     kt.bc(c->g, uout, c->dSc, stage, s);  // the last DETECTION's Boundary_C(Uout)
     c->ctr.kernel_launches += 2;
-    *passes += npass;
-    if (npass > c->ctr.max_passes_stage) c->ctr.max_passes_stage = npass;
     return check_launch(c, "stage");
 }
 
 // SSP_RK3_ (mod_SSP_RK3.f90:12-39) from u into ur; t, dt, qx, qy already on the
 // device.  with_cfl fuses the next step's Setdt into the final combination.
+// One host synchronisation per step, at its end.
 int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
     cudaStream_t s = c->stream;
-    long long passes = 0;
     CU(cudaMemsetAsync(&c->dSc->detected_step, 0, 2 * sizeof(unsigned long long), s));
-    int rc = run_stage(c, u, c->dU1, 0, &passes);
+    int rc = run_stage(c, u, c->dU1, 0);
     if (rc) return rc;
-    rc = run_stage(c, c->dU1, c->dU2, 1, &passes);
+    rc = run_stage(c, c->dU1, c->dU2, 1);
     if (rc) return rc;
     c->kt->combine(c->g, u, c->dU2, 0.75, 0.25, 0, c->dSc, s);  // U2 = 0.75 Uin + 0.25 U2
     c->ctr.kernel_launches += 2;
-    rc = run_stage(c, c->dU2, ur, 2, &passes);
+    rc = run_stage(c, c->dU2, ur, 2);
     if (rc) return rc;
     c->kt->combine(c->g, u, ur, 1. / 3, 2. / 3, with_cfl ? 1 : 0, c->dSc, s);  // Uout = Uin/3 + 2 Uout/3
     rc = check_launch(c, "combine");
     if (rc) return rc;
     CU(cudaMemcpyAsync(c->hSc, c->dSc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
+    CU(cudaMemcpyAsync(c->hBar, c->dBar, sizeof(GridBar), cudaMemcpyDeviceToHost, s));
     CU(cudaStreamSynchronize(s));
+    const bool mood = c->p.method == GPMOOD_GP_MOOD || c->p.method == GPMOOD_NN_GP_MOOD;
+    long long passes = 0;
+    for (int st = 0; st < 3; st++) {
+        const long long np = mood ? c->hSc->passes_stage[st] : 1;
+        passes += np;
+        if (np > c->ctr.max_passes_stage) c->ctr.max_passes_stage = np;
+        if (c->timing) {
+            float f = 0.f, u_ = 0.f, m = 0.f;
+            cudaEventElapsedTime(&f, c->ev[st][0], c->ev[st][1]);
+            cudaEventElapsedTime(&u_, c->ev[st][1], c->ev[st][2]);
+            cudaEventElapsedTime(&m, c->ev[st][2], c->ev[st][3]);
+            c->tm.flux_ms += f;
+            c->tm.flux_launches += 2;
+            c->tm.flux_faces += (long long)(c->p.lf + 1) * c->p.nf + (long long)c->p.lf * (c->p.nf + 1);
+            c->tm.update_ms += u_;
+            c->tm.update_launches += 1;
+            c->tm.mood_ms += m;
+        }
+    }
     c->ctr.detected_last_step = (long long)c->hSc->detected_step;
     c->ctr.a_priori_last_step = (long long)c->hSc->apriori_step;
     c->ctr.detected_total += (long long)c->hSc->detected_step;
     c->ctr.mood_passes_last_step = passes;
     c->ctr.steps++;
     c->ctr.status_flags |= c->hSc->status;
+    if (c->hBar->err) {
+        cudaMemsetAsync(c->dBar, 0, sizeof(GridBar), s);
+        cudaStreamSynchronize(s);
+        return fail(c, GPMOOD_E_CUDA, "MOOD loop: grid barrier timed out");
+    }
+    if (c->hSc->status & GPM_STATUS_MOODCAP) {
+        const long long cap = c->p.max_mood_iters > 0 ? c->p.max_mood_iters : 2LL * c->p.lf * c->p.nf + 2;
+        return fail(c, GPMOOD_E_MOOD_CAP, "MOOD loop did not converge in %lld passes", cap);
+    }
     return 0;
 }
 
@@ -252,8 +252,9 @@ void free_all(gpmood_ctx* c) {
     if (c->hSc) cudaFreeHost(c->hSc);
     if (c->hCount) cudaFreeHost(c->hCount);
     if (c->nn) nn_gate_destroy(c->nn);
-    for (int i = 0; i < 4; i++)
-        if (c->ev[i]) cudaEventDestroy(c->ev[i]);
+    for (int st = 0; st < 3; st++)
+        for (int i = 0; i < 4; i++)
+            if (c->ev[st][i]) cudaEventDestroy(c->ev[st][i]);
     if (c->stream) cudaStreamDestroy(c->stream);
 }
 
@@ -359,8 +360,8 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
         delete c;
         return GPMOOD_E_CUDA;
     }
-    for (int i = 0; i < 4; i++) {
-        if (cudaEventCreate(&c->ev[i]) != cudaSuccess) {
+    for (int i = 0; i < 12; i++) {
+        if (cudaEventCreate(&c->ev[i / 4][i % 4]) != cudaSuccess) {
             fail(c, GPMOOD_E_CUDA, "event creation failed");
             free_all(c);
             delete c;
@@ -380,6 +381,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
         cudaMemsetAsync(c->dU, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dUr, 0, sb, s0) != cudaSuccess ||
         cudaMemsetAsync(c->dU1, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dU2, 0, sb, s0) != cudaSuccess ||
         cudaMemsetAsync(c->dStageOrd, p->mord, 3 * c->ncell, s0) != cudaSuccess ||
+        cudaMemsetAsync(c->dBar, 0, sizeof(GridBar), s0) != cudaSuccess ||
         cudaStreamSynchronize(s0) != cudaSuccess) {
         fail(c, GPMOOD_E_CUDA, "device initialisation failed");
         free_all(c);

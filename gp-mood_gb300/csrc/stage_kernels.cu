@@ -431,9 +431,10 @@ __device__ __forceinline__ bool grid_sync(GridBar* b) {
 
 template <int NGP>
 __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_constant__ GpWeights w, GridBar* bar,
-                                                      int max_pass, unsigned pass_base) {
+                                                      int max_pass, int stage) {
     const GridGeom& g = a.g;
     const double qx = a.sc->qx, qy = a.sc->qy;
+    const unsigned epoch = a.sc->stamp_epoch;  // stamps epoch+2, epoch+3, ... are new
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     const int stid = spread_tid();  // work items are dealt over all SMs
     int cur = 0, pass = 1;  // pass 1 (all faces) ran before this kernel
@@ -465,7 +466,7 @@ __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_
         }
         if (!grid_sync(bar)) return;
         // the 5-point crosses: Uout from Uin and the current fluxes, DETECTION
-        const unsigned pid = pass_base + (unsigned)pass;
+        const unsigned pid = epoch + (unsigned)pass;
         const int nxt = cur ^ 1, total = 5 * nt;
         const int lim = ((total + gstride - 1) / gstride) * gstride;
         for (int base = 0; base < lim; base += gstride) {
@@ -489,11 +490,14 @@ __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_
         if (!grid_sync(bar)) return;
         cur ^= 1;
     }
-    if (gtid == 0) a.sc->passes = pass;
+    if (gtid == 0) {  // every CTA read the epoch before the first barrier
+        a.sc->passes_stage[stage] = pass;
+        a.sc->stamp_epoch = epoch + (unsigned)pass + 1u;
+    }
 }
 
 template <int NGP>
-static int launch_mood_loop_n(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, unsigned pass_base,
+static int launch_mood_loop_n(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, int stage,
                               cudaStream_t s) {
     static int grid = 0;
     if (!grid) {
@@ -505,20 +509,20 @@ static int launch_mood_loop_n(const StageArgs& a, const GpWeights& w, GridBar* b
     }
     StageArgs aa = a;
     GpWeights ww = w;
-    void* args[] = {&aa, &ww, &bar, &max_pass, &pass_base};
+    void* args[] = {&aa, &ww, &bar, &max_pass, &stage};
     return cudaLaunchCooperativeKernel((const void*)k_mood_loop<NGP>, dim3(grid), dim3(256), args, 0, s) == cudaSuccess
                ? 0
                : -1;
 }
 
-int launch_mood_loop(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, unsigned pass_base,
+int launch_mood_loop(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, int stage,
                      cudaStream_t s) {
     switch (a.g.ngp) {
-    case 1: return launch_mood_loop_n<1>(a, w, bar, max_pass, pass_base, s);
-    case 2: return launch_mood_loop_n<2>(a, w, bar, max_pass, pass_base, s);
-    case 3: return launch_mood_loop_n<3>(a, w, bar, max_pass, pass_base, s);
-    case 4: return launch_mood_loop_n<4>(a, w, bar, max_pass, pass_base, s);
-    default: return launch_mood_loop_n<5>(a, w, bar, max_pass, pass_base, s);
+    case 1: return launch_mood_loop_n<1>(a, w, bar, max_pass, stage, s);
+    case 2: return launch_mood_loop_n<2>(a, w, bar, max_pass, stage, s);
+    case 3: return launch_mood_loop_n<3>(a, w, bar, max_pass, stage, s);
+    case 4: return launch_mood_loop_n<4>(a, w, bar, max_pass, stage, s);
+    default: return launch_mood_loop_n<5>(a, w, bar, max_pass, stage, s);
     }
 }
 
