@@ -45,6 +45,7 @@ struct gpmood_batch {
     int2* pblocks = nullptr;
     int npb = 0;
     int tile = 0;
+    bool xy_ok = false;  // the two-direction cell tile applies (fast mode, order 5, ngp 3)
     const BatchTable* bt = nullptr;
     void (*set_max_nx)(int) = nullptr;
     cudaStream_t stream = nullptr;
@@ -208,6 +209,8 @@ int gpmood_batch_create(const gpmood_params* p, int nprob, const int* lf, const 
     b->p = *p;
     b->nprob = nprob;
     b->bt = p->fp_mode == GPMOOD_FP_FAST ? &gpm_fast::batch_table : &gpm_exact::batch_table;
+    b->xy_ok = p->fp_mode == GPMOOD_FP_FAST && p->mord == 5 && p->ngp == 3;
+    b->tile = b->xy_ok ? GPM_TILE_XY : 0;  // the single-problem path's first pass
     b->set_max_nx = p->fp_mode == GPMOOD_FP_FAST ? gpm_fast::batch_set_max_nx : gpm_exact::batch_set_max_nx;
 
     // problems, weight classes (one GP weight set per distinct grid size)
@@ -252,7 +255,11 @@ int gpmood_batch_create(const gpmood_params* p, int nprob, const int* lf, const 
         return (long long)lf[x] * nf[x] > (long long)lf[y] * nf[y];
     });
     std::vector<int4> ft[GPM_NTILES];
-    for (int k = 0; k < GPM_NTILES; k++)
+    for (int i : ord)  // two-direction cell tiles over [0,lf] x [0,nf]
+        for (int n0 = 0; n0 <= nf[i]; n0 += kTileTY[GPM_TILE_XY])
+            for (int l0 = 0; l0 <= lf[i]; l0 += kTileTX[GPM_TILE_XY]) ft[GPM_TILE_XY].push_back(make_int4(i, 2, l0, n0));
+    for (int k = 0; k < GPM_NTILES; k++) {
+        if (k == GPM_TILE_XY) continue;
         for (int i : ord) {
             const int TX = kTileTX[k], TY = kTileTY[k];
             for (int n0 = 1; n0 <= nf[i]; n0 += TY)
@@ -260,6 +267,7 @@ int gpmood_batch_create(const gpmood_params* p, int nprob, const int* lf, const 
             for (int n0 = 0; n0 <= nf[i]; n0 += TY)
                 for (int l0 = 1; l0 <= lf[i]; l0 += TX) ft[k].push_back(make_int4(i, 1, l0, n0));
         }
+    }
     std::vector<int2> cb, pb;
     for (int i : ord) {
         for (int k = 0; k < lf[i] * nf[i]; k += 256) cb.push_back(make_int2(i, k));
@@ -414,6 +422,10 @@ int gpmood_batch_autotune(gpmood_batch* b, int* tile, double* ms_per_tile) {
     int best = 0;
     float best_ms = 1e30f;
     for (int k = 0; k < GPM_NTILES; k++) {
+        if (k == GPM_TILE_XY && !b->xy_ok) {
+            if (ms_per_tile) ms_per_tile[k] = 0.0;
+            continue;
+        }
         b->tile = k;
         const BatchArgs a = make_args(b, u, b->U1, 0);
         b->bt->flux(a, s);  // warm-up

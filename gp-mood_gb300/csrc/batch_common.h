@@ -50,10 +50,13 @@ struct BatchArgs {
     int tile;             // face-tile shape index chosen by the autotuner
 };
 
-// Face-tile shapes (TX x TY faces per CTA) the autotuner chooses from.
-#define GPM_NTILES 4
-static const int kTileTX[GPM_NTILES] = {32, 32, 16, 64};
-static const int kTileTY[GPM_NTILES] = {8, 4, 16, 4};
+// Face-tile shapes (TX x TY faces per CTA) the autotuner chooses from.  The
+// last one is the fast mode's two-direction cell tile (order 5, ngp = 3
+// only): items (problem, 2, l0, n0) over cells [0,lf] x [0,nf].
+#define GPM_NTILES 5
+#define GPM_TILE_XY 4
+static const int kTileTX[GPM_NTILES] = {32, 32, 16, 64, 32};
+static const int kTileTY[GPM_NTILES] = {8, 4, 16, 4, 8};
 
 struct BatchTable {
     void (*bc)(const BatchArgs& a, double* u, cudaStream_t s);

@@ -232,6 +232,33 @@ extern "C" int gpm_gp_presim(double ell_o_dx, double lx, double ly, int lf, int 
                 }
             }
         }
+        // orbit components of the left (x) and bottom (y) faces at order 5;
+        // stencil indices: 0 (0,0), 1 (-1,0), 2 (0,1), 3 (1,0), 4 (0,-1),
+        // 5 (-1,-1), 6 (-1,1), 7 (1,1), 8 (1,-1), 9 (0,-2), 10 (-2,0), 11 (0,2), 12 (2,0)
+        auto split = [](const double* z, double* c13) {
+            const double za = z[5], zb = z[8], zc = z[6], zd = z[7];
+            c13[0] = z[0];
+            c13[1] = 0.5 * (z[1] + z[3]);
+            c13[2] = 0.5 * (z[10] + z[12]);
+            c13[3] = 0.5 * (z[4] + z[2]);
+            c13[4] = 0.5 * (z[9] + z[11]);
+            c13[5] = 0.25 * (za + zb + zc + zd);
+            c13[6] = 0.5 * (z[1] - z[3]);
+            c13[7] = 0.5 * (z[10] - z[12]);
+            c13[8] = 0.25 * (za - zb + zc - zd);
+            c13[9] = 0.5 * (z[4] - z[2]);
+            c13[10] = 0.5 * (z[9] - z[11]);
+            c13[11] = 0.25 * (za + zb - zc - zd);
+            c13[12] = 0.25 * (za - zb - zc + zd);
+        };
+        double c[13];
+        split(out->zt[2][0][0], out->orb.x0);
+        split(out->zt[2][0][1], c);
+        for (int k = 0; k < 9; k++) out->orb.x1[k] = c[k];  // y-symmetric: groups 3, 4 vanish
+        split(out->zt[2][3][0], out->orb.y0);
+        split(out->zt[2][3][1], c);
+        for (int k = 0; k < 6; k++) out->orb.y1[k] = c[k];  // x-symmetric: groups 2, 4 vanish
+        for (int k = 0; k < 3; k++) out->orb.y1[6 + k] = c[9 + k];
     }
     return 0;
 }

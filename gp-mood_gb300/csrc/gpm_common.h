@@ -34,6 +34,23 @@ __host__ __device__ constexpr int gpm_sym_pair(int dir, int k, int side) {
     return dir == 0 ? (k == 0 ? (side ? 4 : 2) : k == 1 ? (side ? 5 : 6) : k == 2 ? (side ? 8 : 7) : (side ? 9 : 11))
                     : (k == 0 ? (side ? 3 : 1) : k == 1 ? (side ? 8 : 5) : k == 2 ? (side ? 7 : 6) : (side ? 12 : 10));
 }
+// Weights of a whole cell's face states on the symmetry components of its
+// 13-point stencil (ngp = 3, order 5; fast first pass).  Under the mirrors
+// x -> -x and y -> -y the stencil splits into orbits whose values combine
+// into components Q: Q0 = q(0,0); Q1p/Q1m = q(-1,0) +/- q(1,0);
+// Q2p/Q2m = q(-2,0) +/- q(2,0); Q3p/Q3m = q(0,-1) +/- q(0,1);
+// Q4p/Q4m = q(0,-2) +/- q(0,2); for the corners a=(-1,-1), b=(1,-1),
+// c=(-1,1), d=(1,1): Q5pp = a+b+c+d, Q5mp = (a-b)+(c-d), Q5pm = (a+b)-(c+d),
+// Q5mm = (a-b)-(c-d).  x0 weighs them for the left face at Gauss point 0 in
+// the order [Q0 Q1p Q2p Q3p Q4p Q5pp | Q1m Q2m Q5mp | Q3m Q4m Q5pm | Q5mm];
+// the right face and Gauss point 2 follow by sign changes of the groups.  x1
+// (Gauss point 1, on the face's axis) has [Q0 Q1p Q2p Q3p Q4p Q5pp | Q1m Q2m
+// Q5mp].  y0/y1 do the same for the bottom face, with y1's second group
+// [Q3m Q4m Q5pm].
+struct GpOrbit {
+    double x0[13], x1[9], y0[13], y1[9];
+};
+
 struct GpSym {
     double a0[5], a1[5];         // axis weights of Gauss points 0 and 1
     double al[4], be[4], ga[4];  // per pair: (z0_m + z0_m')/2, (z0_m - z0_m')/2, z1_m
@@ -46,6 +63,7 @@ struct GpWeights {
     double gw[GPM_MAXGP];            // gauss_weight(ngp, :)
     double d2x[5], d2y[5];           // GP_d2x_sp(3,:), GP_d2y_sp(3,:)
     GpSym sym[3][4];                 // ngp = 3 split of zt (fast mode); zero otherwise
+    GpOrbit orb;                     // ngp = 3 order-5 cell-wise split (fast mode); zero otherwise
 };
 
 struct GridGeom {

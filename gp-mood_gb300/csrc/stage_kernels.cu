@@ -202,6 +202,194 @@ __global__ void __launch_bounds__(TX * TY) k_flux_tile(StageArgs a, const __grid
     st_cell(out, Cell{F[0], F[1], F[2], F[3]});
 }
 
+#if !GPM_EXACT
+// ---------------------------------------------------------------------------
+// Fast first pass at uniform order 5 with ngp = 3: both face directions of a
+// tile of cells in one CTA.  Every cell's 12 face states (left/right/bottom/
+// top faces at 3 Gauss points) come from the mirror-symmetry components of its
+// 13-point stencil (GpOrbit): 16 operations form the components, 32 give the
+// six x-face states and 32 the six y-face states, per variable -- 80 FP64
+// operations for 12 states, against 128 when each face gathers its two states
+// on its own.  A cell keeps its right and top states in registers and passes
+// its left and bottom states to its neighbours through shared memory; then
+// every thread solves the x face and the y face of which its cell is the low
+// side.  The tile owns cells (l0..l0+XT-1, n0..n0+XY-1) of l in [0,lf],
+// n in [0,nf]; one extra column (left states) and row (bottom states) is
+// computed by two warps.
+constexpr int XT = 32, XY = 8;          // cells per tile
+constexpr int XS = 13;                  // doubles per published state set (12 used, padded)
+
+struct XyOut {
+    double lo[3][4];  // left (x) or bottom (y) face states
+    double hi[3][4];  // right (x) or top (y) face states
+};
+
+__device__ __forceinline__ double tile_var(const Cell* t, int k) { return cell_var(*t, k); }
+
+// Components of the stencil values of variable k around tile position (cx, cy).
+struct Comp {
+    double v[13];  // [Q0 Q1p Q2p Q3p Q4p Q5pp Q1m Q2m Q5mp Q3m Q4m Q5pm Q5mm]
+};
+
+__device__ __forceinline__ void components(const Cell (*tile)[XT + 5], int cx, int cy, int k, Comp& c) {
+    auto q = [&](int ox, int oy) { return cell_var(tile[cy + oy][cx + ox], k); };
+    const double qm1 = q(-1, 0), qp1 = q(1, 0), qm2 = q(-2, 0), qp2 = q(2, 0);
+    const double qb1 = q(0, -1), qt1 = q(0, 1), qb2 = q(0, -2), qt2 = q(0, 2);
+    const double a = q(-1, -1), b = q(1, -1), cc = q(-1, 1), d = q(1, 1);
+    c.v[0] = q(0, 0);
+    c.v[1] = qm1 + qp1;
+    c.v[2] = qm2 + qp2;
+    c.v[3] = qb1 + qt1;
+    c.v[4] = qb2 + qt2;
+    const double s1 = a + b, s2 = cc + d, d1 = a - b, d2 = cc - d;
+    c.v[5] = s1 + s2;
+    c.v[6] = qm1 - qp1;
+    c.v[7] = qm2 - qp2;
+    c.v[8] = d1 + d2;
+    c.v[9] = qb1 - qt1;
+    c.v[10] = qb2 - qt2;
+    c.v[11] = s1 - s2;
+    c.v[12] = d1 - d2;
+}
+
+// x family: left (lo) and right (hi) face states at Gauss points 0, 1, 2.
+__device__ __forceinline__ void x_family(const GpOrbit& o, const Comp& c, int k, XyOut& r) {
+    const double Ppp = o.x0[0] * c.v[0] + o.x0[1] * c.v[1] + o.x0[2] * c.v[2] + o.x0[3] * c.v[3] +
+                       o.x0[4] * c.v[4] + o.x0[5] * c.v[5];
+    const double Pmp = o.x0[6] * c.v[6] + o.x0[7] * c.v[7] + o.x0[8] * c.v[8];
+    const double Ppm = o.x0[9] * c.v[9] + o.x0[10] * c.v[10] + o.x0[11] * c.v[11];
+    const double Pmm = o.x0[12] * c.v[12];
+    const double A = Ppp + Ppm, B = Pmp + Pmm, C = Ppp - Ppm, D = Pmp - Pmm;
+    r.lo[0][k] = A + B;
+    r.hi[0][k] = A - B;
+    r.lo[2][k] = C + D;
+    r.hi[2][k] = C - D;
+    const double P1pp = o.x1[0] * c.v[0] + o.x1[1] * c.v[1] + o.x1[2] * c.v[2] + o.x1[3] * c.v[3] +
+                        o.x1[4] * c.v[4] + o.x1[5] * c.v[5];
+    const double P1mp = o.x1[6] * c.v[6] + o.x1[7] * c.v[7] + o.x1[8] * c.v[8];
+    r.lo[1][k] = P1pp + P1mp;
+    r.hi[1][k] = P1pp - P1mp;
+}
+
+// y family: bottom (lo) and top (hi) face states at Gauss points 0, 1, 2.
+__device__ __forceinline__ void y_family(const GpOrbit& o, const Comp& c, int k, XyOut& r) {
+    const double Ppp = o.y0[0] * c.v[0] + o.y0[1] * c.v[1] + o.y0[2] * c.v[2] + o.y0[3] * c.v[3] +
+                       o.y0[4] * c.v[4] + o.y0[5] * c.v[5];
+    const double Pmp = o.y0[6] * c.v[6] + o.y0[7] * c.v[7] + o.y0[8] * c.v[8];
+    const double Ppm = o.y0[9] * c.v[9] + o.y0[10] * c.v[10] + o.y0[11] * c.v[11];
+    const double Pmm = o.y0[12] * c.v[12];
+    const double A = Ppp + Ppm, B = Pmp + Pmm, C = Ppp - Ppm, D = Pmp - Pmm;
+    r.lo[0][k] = A + B;
+    r.lo[2][k] = A - B;
+    r.hi[0][k] = C + D;
+    r.hi[2][k] = C - D;
+    const double P1pp = o.y1[0] * c.v[0] + o.y1[1] * c.v[1] + o.y1[2] * c.v[2] + o.y1[3] * c.v[3] +
+                        o.y1[4] * c.v[4] + o.y1[5] * c.v[5];
+    const double P1pm = o.y1[6] * c.v[9] + o.y1[7] * c.v[10] + o.y1[8] * c.v[11];
+    r.lo[1][k] = P1pp + P1pm;
+    r.hi[1][k] = P1pp - P1pm;
+}
+
+__device__ __forceinline__ void publish(double* dst, const double (*st)[4]) {
+#pragma unroll
+    for (int g = 0; g < 3; g++)
+#pragma unroll
+        for (int k = 0; k < 4; k++) dst[4 * g + k] = st[g][k];
+}
+
+struct XySmem {
+    Cell tile[XY + 5][XT + 5];
+    double left[XY][XT][XS];    // left-face states of cells l0+1 .. l0+XT
+    double bottom[XY][XT][XS];  // bottom-face states of rows n0+1 .. n0+XY
+};
+
+__device__ __forceinline__ void xy_tile(const GridGeom& g, const GpWeights& w, const double* __restrict__ uin,
+                                        double* __restrict__ fx, double* __restrict__ fy, int l0, int n0,
+                                        XySmem& sm) {
+    const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * XT + tx;
+    for (int i = tid; i < (XT + 5) * (XY + 5); i += XT * XY) {
+        const int cy = i / (XT + 5), cx = i - cy * (XT + 5);
+        const int l = l0 - 2 + cx, n = n0 - 2 + cy;
+        if (l >= -3 && l <= g.lf + 4 && n >= -3 && n <= g.nf + 4) sm.tile[cy][cx] = ld_cell(uin + 4 * cidx(g, l, n));
+    }
+    __syncthreads();
+    const int l = l0 + tx, n = n0 + ty;
+    // a cell up to (lf+1, nf+1) provides states: its stencil stays inside the padded grid
+    const bool live = l <= g.lf + 1 && n <= g.nf + 1;
+    XyOut xs, ys;
+    if (live) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            Comp c;
+            components(sm.tile, tx + 2, ty + 2, k, c);
+            x_family(w.orb, c, k, xs);
+            y_family(w.orb, c, k, ys);
+        }
+        if (tx > 0) publish(sm.left[ty][tx - 1], xs.lo);
+        if (ty > 0) publish(sm.bottom[ty - 1][tx], ys.lo);
+    }
+    // the extra column (left states of cells l0+XT) and row (bottom states of n0+XY)
+    if (ty == XY - 1 && l <= g.lf + 1 && n0 + XY <= g.nf + 1) {
+        XyOut e;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            Comp c;
+            components(sm.tile, tx + 2, XY + 2, k, c);
+            y_family(w.orb, c, k, e);
+        }
+        publish(sm.bottom[XY - 1][tx], e.lo);
+    }
+    if (ty == XY - 2 && tx < XY && l0 + XT <= g.lf + 1 && n0 + tx <= g.nf + 1) {
+        XyOut e;
+#pragma unroll
+        for (int k = 0; k < 4; k++) {
+            Comp c;
+            components(sm.tile, XT + 2, tx + 2, k, c);
+            x_family(w.orb, c, k, e);
+        }
+        publish(sm.left[tx][XT - 1], e.lo);
+    }
+    __syncthreads();
+    if (l <= g.lf && n >= 1 && n <= g.nf) {  // x face between (l,n) and (l+1,n)
+        double uR[3][4], F[4];
+        const double* src = sm.left[ty][tx];
+#pragma unroll
+        for (int gp = 0; gp < 3; gp++)
+#pragma unroll
+            for (int k = 0; k < 4; k++) uR[gp][k] = src[4 * gp + k];
+        quad_flux<0, 3>(xs.hi, uR, w.gw, F);
+        st_cell(fx + 4 * cidx(g, l, n), Cell{F[0], F[1], F[2], F[3]});
+    }
+    if (l >= 1 && l <= g.lf && n <= g.nf) {  // y face between (l,n) and (l,n+1)
+        double uR[3][4], F[4];
+        const double* src = sm.bottom[ty][tx];
+#pragma unroll
+        for (int gp = 0; gp < 3; gp++)
+#pragma unroll
+            for (int k = 0; k < 4; k++) uR[gp][k] = src[4 * gp + k];
+        quad_flux<1, 3>(ys.hi, uR, w.gw, F);
+        st_cell(fy + 4 * cidx(g, l, n), Cell{F[0], F[1], F[2], F[3]});
+    }
+}
+
+__global__ void __launch_bounds__(XT * XY) k_flux_xy(StageArgs a, const __grid_constant__ GpWeights w) {
+    extern __shared__ __align__(16) unsigned char xy_raw[];
+    XySmem& sm = *reinterpret_cast<XySmem*>(xy_raw);
+    xy_tile(a.g, w, a.uin, a.fx, a.fy, blockIdx.x * XT, blockIdx.y * XY, sm);
+}
+
+bool launch_flux_xy(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
+    static bool attr = false;
+    if (!attr) {
+        cudaFuncSetAttribute(k_flux_xy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(XySmem));
+        attr = true;
+    }
+    const dim3 grid((a.g.lf + 1 + XT - 1) / XT, (a.g.nf + 1 + XY - 1) / XY), blk(XT, XY);
+    k_flux_xy<<<grid, blk, sizeof(XySmem), s>>>(a, w);
+    return true;
+}
+#endif
+
 template <int DIR, int NGP>
 void launch_flux_dir(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
     const int nl = DIR == 0 ? a.g.lf + 1 : a.g.lf;
@@ -220,6 +408,9 @@ void launch_flux_ngp(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
 }
 
 void launch_flux_all(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
+#if !GPM_EXACT
+    if (a.uniform_order && a.g.mord == 5 && a.g.ngp == 3 && launch_flux_xy(a, w, s)) return;
+#endif
     switch (a.g.ngp) {
     case 1: launch_flux_ngp<1>(a, w, s); break;
     case 2: launch_flux_ngp<2>(a, w, s); break;
@@ -771,6 +962,20 @@ __global__ void __launch_bounds__(TXB* TYB) kb_flux(BatchArgs a) {
     }
 }
 
+#if !GPM_EXACT
+// The two-direction cell tiles of every problem (xy_tile), persistent CTAs.
+__global__ void __launch_bounds__(XT * XY) kb_flux_xy(BatchArgs a) {
+    extern __shared__ __align__(16) unsigned char xy_raw[];
+    XySmem& sm = *reinterpret_cast<XySmem*>(xy_raw);
+    for (int item = blockIdx.x; item < a.nftiles; item += gridDim.x) {
+        const int4 it = a.ftiles[item];
+        const BProb P = a.prob[it.x];
+        __syncthreads();  // the previous tile is done with the shared buffers
+        xy_tile(bgeom(a, P), a.wtab[P.wc], a.uin + 4 * P.off, a.fx + 4 * P.off, a.fy + 4 * P.off, it.z, it.w, sm);
+    }
+}
+#endif
+
 static int g_sms = 0;
 static int sm_count() {
     if (!g_sms) {
@@ -792,6 +997,18 @@ static void blaunch_flux_t(const BatchArgs& a, cudaStream_t s) {
 
 template <int NGP>
 static void blaunch_flux_n(const BatchArgs& a, cudaStream_t s) {
+#if !GPM_EXACT
+    if (a.tile == GPM_TILE_XY && NGP == 3 && a.mord == 5) {
+        static bool attr = false;
+        if (!attr) {
+            cudaFuncSetAttribute(kb_flux_xy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(XySmem));
+            attr = true;
+        }
+        const int grid = a.nftiles < sm_count() * 2 ? a.nftiles : sm_count() * 2;
+        kb_flux_xy<<<grid, dim3(XT, XY), sizeof(XySmem), s>>>(a);
+        return;
+    }
+#endif
     switch (a.tile) {
     case 0: blaunch_flux_t<32, 8, NGP>(a, s); break;
     case 1: blaunch_flux_t<32, 4, NGP>(a, s); break;

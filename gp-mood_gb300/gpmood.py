@@ -466,7 +466,7 @@ class Batch:
 
     def autotune(self):
         k = C.c_int()
-        ms = np.zeros(4)
+        ms = np.zeros(5)  # one time per tile shape (gpmood_batch_autotune)
         self._check(self.lib.gpmood_batch_autotune(self._h, C.byref(k), _dp(ms)))
         return k.value, ms
 

@@ -195,7 +195,10 @@ int  gpmood_batch_get_state(gpmood_batch* b, int i, double* u_host, double* t);
 /* nsteps steps of every problem (Setdt + time_stepping + t += dt each). */
 int  gpmood_batch_advance(gpmood_batch* b, int nsteps);
 /* Time each face-tile shape on this batch and keep the fastest: *tile gets its
- * index, ms_per_tile[4] (may be NULL) the measured times. */
+ * index, ms_per_tile[5] (may be NULL) the measured times.  Shapes 0-3 are
+ * one-direction face tiles (32x8, 32x4, 16x16, 64x4); shape 4 is the fast
+ * mode's two-direction cell tile (order 5, ngp 3 only; time 0 otherwise),
+ * which is also the default there. */
 int  gpmood_batch_autotune(gpmood_batch* b, int* tile, double* ms_per_tile);
 /* Interior cells of all problems, steps taken, detected cells (all steps),
  * status bits, and 1 if steps replay a CUDA graph (-1: eager launches). */

@@ -52,7 +52,7 @@ def test_autotune_keeps_results(pkg):
                 b.set_state(i, U, 0.0)
             if tune:
                 k, ms = b.autotune()
-                assert 0 <= k < 4 and np.all(ms > 0)
+                assert 0 <= k < 4 and np.all(ms[:4] > 0) and ms[4] == 0  # exact mode: no cell tile
             b.advance(4)
             finals.append([b.get_state(i)[0] for i in range(len(probs))])
             graphed = b.stats()["graphed"]
