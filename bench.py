@@ -469,7 +469,9 @@ def run_ours(args, ws, rank, local):
     achieved_tflops = FLOPS_PER_FACE * faces_per_launch / (launch_ms * 1e-3) / 1e12
     peak_tflops = peak_fp64_gflops / 1e3
     tpf = ncu_traffic_per_face()
-    roofline = {"bound": "fp64", "kernel": "k_flux_tile (GP recon + HLLC + quadrature)",
+    kname = ("k_flux_xy (both face directions: GP recon + HLLC + quadrature)" if fp == pkg.FP_FAST
+             else "k_flux_tile (GP recon + HLLC + quadrature)")
+    roofline = {"bound": "fp64", "kernel": kname,
                 "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
                 "frac": achieved_tflops / peak_tflops,
                 "traffic": (tpf * faces_per_launch) if tpf else None,

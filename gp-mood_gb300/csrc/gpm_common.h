@@ -114,7 +114,7 @@ struct StageArgs {
 // (stage_kernels.cu compiled with and without FMA contraction).
 struct KernelTable {
     void (*bc)(const GridGeom& g, double* u, const DevScalars* sc, int stage, cudaStream_t s);
-    void (*flux_all)(const StageArgs& a, const GpWeights& w, cudaStream_t s);
+    int (*flux_all)(const StageArgs& a, const GpWeights& w, cudaStream_t s);  // returns the launches made
     void (*update_detect)(const StageArgs& a, const GpWeights& w, int cur, cudaStream_t s);
     void (*mood_mark)(const StageArgs& a, int cur, int max_trb, cudaStream_t s);
     void (*mood_faces)(const StageArgs& a, const GpWeights& w, int cur, int max_trb, cudaStream_t s);

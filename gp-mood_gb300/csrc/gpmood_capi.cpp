@@ -49,6 +49,7 @@ struct gpmood_ctx {
     bool timing;                  // per-kernel CUDA-event timing
     bool trace;                   // GPMOOD_TRACE=1: one line per step on stderr
     cudaEvent_t ev[3][4];         // per RK stage: flux, update, MOOD loop boundaries
+    int flux_nl[3];               // first-pass face launches of each RK stage
     gpmood_timing tm;
     char err[512];
 };
@@ -126,7 +127,7 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage) {
     // flux the value of a first pass at the gated orders.
     StageArgs au = a;
     au.uniform_order = 1;
-    kt.flux_all(au, c->w, s);
+    c->flux_nl[stage] = kt.flux_all(au, c->w, s);
     if (!uniform) {
         kt.mood_faces(a, c->w, 1, c->p.lf * c->p.nf, s);
         c->ctr.kernel_launches += 1;
@@ -134,7 +135,7 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage) {
     if (c->timing) cudaEventRecord(ev[1], s);
     kt.update_detect(a, c->w, 0, s);
     if (c->timing) cudaEventRecord(ev[2], s);
-    c->ctr.kernel_launches += 3;
+    c->ctr.kernel_launches += 1 + c->flux_nl[stage];
     int rc = check_launch(c, "first MOOD pass");
     if (rc) return rc;
     if (c->p.method == GPMOOD_GP_MOOD || c->p.method == GPMOOD_NN_GP_MOOD) {
@@ -191,7 +192,7 @@ int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
             cudaEventElapsedTime(&u_, c->ev[st][1], c->ev[st][2]);
             cudaEventElapsedTime(&m, c->ev[st][2], c->ev[st][3]);
             c->tm.flux_ms += f;
-            c->tm.flux_launches += 2;
+            c->tm.flux_launches += c->flux_nl[st];
             c->tm.flux_faces += (long long)(c->p.lf + 1) * c->p.nf + (long long)c->p.lf * (c->p.nf + 1);
             c->tm.update_ms += u_;
             c->tm.update_launches += 1;

@@ -407,9 +407,9 @@ void launch_flux_ngp(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
     launch_flux_dir<1, NGP>(a, w, s);
 }
 
-void launch_flux_all(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
+int launch_flux_all(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
 #if !GPM_EXACT
-    if (a.uniform_order && a.g.mord == 5 && a.g.ngp == 3 && launch_flux_xy(a, w, s)) return;
+    if (a.uniform_order && a.g.mord == 5 && a.g.ngp == 3 && launch_flux_xy(a, w, s)) return 1;
 #endif
     switch (a.g.ngp) {
     case 1: launch_flux_ngp<1>(a, w, s); break;
@@ -418,6 +418,7 @@ void launch_flux_all(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
     case 4: launch_flux_ngp<4>(a, w, s); break;
     default: launch_flux_ngp<5>(a, w, s); break;
     }
+    return 2;
 }
 
 // ---------------------------------------------------------------------------
@@ -454,14 +455,24 @@ __device__ __forceinline__ void list_append(bool flag, int* __restrict__ list, i
     if (flag) list[base + __popc(m & ((1u << lane) - 1))] = value;
 }
 
-// Position of the calling thread in an order that deals consecutive work
-// items round-robin over the CTAs (one or a few per SM) and, inside a CTA,
-// over its warps (the SM's sub-partitions).  A short list then spreads over
-// every SM's FP64 units instead of filling the first few CTAs.  Lanes of one
-// warp get items that differ by a multiple of 4 * (number of warps).
-__device__ __forceinline__ int spread_tid() {
-    const int nw = blockDim.x >> 5;
-    return (threadIdx.x & 31) * (gridDim.x * nw) + (threadIdx.x >> 5) * gridDim.x + blockIdx.x;
+// Position of the calling thread in an order that fills whole warps with
+// consecutive work items and deals the warps round-robin over the CTAs (one
+// or a few per SM).  An FP64 instruction costs the SM the same time whether
+// 1 or 32 lanes of the warp are active, so a short list must pack its items
+// into as few warps as possible, and spread those warps over the SMs.
+__device__ __forceinline__ int pack_tid() {
+    return (((threadIdx.x >> 5) * gridDim.x + blockIdx.x) << 5) + (threadIdx.x & 31);
+}
+
+// Face item i of the 4*nt faces of nt troubled cells: the x faces come first
+// (item 2j: left face of cell j, 2j+1: its right face), then the y faces
+// (below, above), so the lanes of a warp share one direction.
+__device__ __forceinline__ int face_item(int i, int nt, int* dir, int* side) {
+    const int x = i < 2 * nt ? 1 : 0;
+    const int j = x ? i : i - 2 * nt;
+    *dir = x ? 0 : 1;
+    *side = j & 1;
+    return j >> 1;
 }
 
 __global__ void __launch_bounds__(256) k_update_detect(StageArgs a, const __grid_constant__ GpWeights w, int cur) {
@@ -543,13 +554,12 @@ __device__ __forceinline__ void face_any_order(const StageArgs& a, const GpWeigh
 template <int NGP>
 __global__ void __launch_bounds__(128) k_mood_faces(StageArgs a, const __grid_constant__ GpWeights w, int cur) {
     const int nt = a.sc->ntrb[cur];
-    // 4 faces per troubled cell: x faces (l-1,n), (l,n), y faces (l,n-1), (l,n);
-    // the lanes of a warp get items of one direction (spread_tid).
-    for (int i = spread_tid(); i < 4 * nt; i += gridDim.x * blockDim.x) {
-        const size_t c = (size_t)a.tlist[cur][i >> 2];
-        const int f = i & 3;
-        if ((f & 1) == 0) face_any_order<0, NGP>(a, w, f == 0 ? c - 1 : c);
-        else face_any_order<1, NGP>(a, w, f == 1 ? c - a.g.nx : c);
+    // 4 faces per troubled cell: x faces (l-1,n), (l,n), y faces (l,n-1), (l,n)
+    for (int i = pack_tid(); i < 4 * nt; i += gridDim.x * blockDim.x) {
+        int dir, side;
+        const size_t c = (size_t)a.tlist[cur][face_item(i, nt, &dir, &side)];
+        if (dir == 0) face_any_order<0, NGP>(a, w, side == 0 ? c - 1 : c);
+        else face_any_order<1, NGP>(a, w, side == 0 ? c - a.g.nx : c);
     }
 }
 
@@ -564,7 +574,7 @@ __global__ void __launch_bounds__(256) k_mood_cells(StageArgs a, const __grid_co
     // Round the trip count up to a multiple of the stride so whole warps reach
     // list_append together.
     const int lim = ((total + stride - 1) / stride) * stride;
-    const int st = spread_tid();
+    const int st = pack_tid();
     for (int base = 0; base < lim; base += stride) {
         const int i = base + st;
         bool trb = false;
@@ -627,7 +637,7 @@ __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_
     const double qx = a.sc->qx, qy = a.sc->qy;
     const unsigned epoch = a.sc->stamp_epoch;  // stamps epoch+2, epoch+3, ... are new
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
-    const int stid = spread_tid();  // work items are dealt over all SMs
+    const int stid = pack_tid();  // whole warps of work items, dealt over all SMs
     int cur = 0, pass = 1;  // pass 1 (all faces) ran before this kernel
     for (;;) {
         const int nt = *(volatile int*)&a.sc->ntrb[cur];
@@ -650,10 +660,10 @@ __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_
         if (!grid_sync(bar)) return;
         // the four faces of every troubled cell at the new orders
         for (int i = stid; i < 4 * nt; i += gstride) {
-            const size_t c = (size_t)a.tlist[cur][i >> 2];
-            const int f = i & 3;
-            if ((f & 1) == 0) face_any_order<0, NGP>(a, w, f == 0 ? c - 1 : c);
-            else face_any_order<1, NGP>(a, w, f == 1 ? c - g.nx : c);
+            int dir, side;
+            const size_t c = (size_t)a.tlist[cur][face_item(i, nt, &dir, &side)];
+            if (dir == 0) face_any_order<0, NGP>(a, w, side == 0 ? c - 1 : c);
+            else face_any_order<1, NGP>(a, w, side == 0 ? c - g.nx : c);
         }
         if (!grid_sync(bar)) return;
         // the 5-point crosses: Uout from Uin and the current fluxes, DETECTION
@@ -1088,8 +1098,9 @@ __global__ void kb_mood_mark(BatchArgs a, int cur) {
 template <int NGP>
 __global__ void __launch_bounds__(128) kb_mood_faces(BatchArgs a, int cur) {
     const int nt = a.ntrb[cur];
-    for (int i = spread_tid(); i < 4 * nt; i += gridDim.x * blockDim.x) {
-        const int2 e = a.tlist[cur][i >> 2];
+    for (int i = pack_tid(); i < 4 * nt; i += gridDim.x * blockDim.x) {
+        int dir, side;
+        const int2 e = a.tlist[cur][face_item(i, nt, &dir, &side)];
         const BProb P = a.prob[e.x];
         StageArgs sa;
         sa.g = bgeom(a, P);
@@ -1099,9 +1110,8 @@ __global__ void __launch_bounds__(128) kb_mood_faces(BatchArgs a, int cur) {
         sa.order = a.order + P.off;
         const GpWeights& w = a.wtab[P.wc];
         const size_t c = (size_t)e.y;
-        const int f = i & 3;
-        if ((f & 1) == 0) face_any_order<0, NGP>(sa, w, f == 0 ? c - 1 : c);
-        else face_any_order<1, NGP>(sa, w, f == 1 ? c - sa.g.nx : c);
+        if (dir == 0) face_any_order<0, NGP>(sa, w, side == 0 ? c - 1 : c);
+        else face_any_order<1, NGP>(sa, w, side == 0 ? c - sa.g.nx : c);
     }
 }
 
@@ -1113,7 +1123,7 @@ __global__ void __launch_bounds__(256) kb_mood_cells(BatchArgs a, int cur) {
     const int total = 5 * nt;
     const int stride = gridDim.x * blockDim.x;
     const int lim = ((total + stride - 1) / stride) * stride;
-    const int st = spread_tid();
+    const int st = pack_tid();
     for (int base = 0; base < lim; base += stride) {
         const int i = base + st;
         bool trb = false;
@@ -1159,7 +1169,7 @@ void blaunch_mood_pass(const BatchArgs& a, int cur, cudaStream_t s) {
 template <int NGP>
 __global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar, int max_pass) {
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
-    const int stid = spread_tid();
+    const int stid = pack_tid();
     int cur = 0, pass = 1;
     for (;;) {
         const int nt = *(volatile int*)&a.ntrb[cur];
@@ -1182,7 +1192,8 @@ __global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar
         }
         if (!grid_sync(bar)) return;
         for (int i = stid; i < 4 * nt; i += gstride) {
-            const int2 e = a.tlist[cur][i >> 2];
+            int dir, side;
+            const int2 e = a.tlist[cur][face_item(i, nt, &dir, &side)];
             const BProb P = a.prob[e.x];
             StageArgs sa;
             sa.g = bgeom(a, P);
@@ -1192,9 +1203,8 @@ __global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar
             sa.order = a.order + P.off;
             const GpWeights& w = a.wtab[P.wc];
             const size_t c = (size_t)e.y;
-            const int f = i & 3;
-            if ((f & 1) == 0) face_any_order<0, NGP>(sa, w, f == 0 ? c - 1 : c);
-            else face_any_order<1, NGP>(sa, w, f == 1 ? c - sa.g.nx : c);
+            if (dir == 0) face_any_order<0, NGP>(sa, w, side == 0 ? c - 1 : c);
+            else face_any_order<1, NGP>(sa, w, side == 0 ? c - sa.g.nx : c);
         }
         if (!grid_sync(bar)) return;
         const unsigned epoch = (unsigned)*(volatile int*)&a.ntrb[2];
