@@ -464,13 +464,16 @@ def run_ours(args, ws, rank, local):
     solver.close()
 
     # ---- roofline of the dominant kernel (first-pass face kernel) ----
+    # one "launch" of the roofline = the first pass of one RK stage: every face
+    # of the grid (fast mode: k_flux_xy + k_flux_edge; exact: the x and y kernels)
     launch_ms = tm.flux_ms / max(tm.flux_launches, 1)
     faces_per_launch = tm.flux_faces / max(tm.flux_launches, 1)
     achieved_tflops = FLOPS_PER_FACE * faces_per_launch / (launch_ms * 1e-3) / 1e12
     peak_tflops = peak_fp64_gflops / 1e3
     tpf = ncu_traffic_per_face()
-    kname = ("k_flux_xy (both face directions: GP recon + HLLC + quadrature)" if fp == pkg.FP_FAST
-             else "k_flux_tile (GP recon + HLLC + quadrature)")
+    kname = ("first pass of one RK stage: k_flux_xy (interior, both directions) + k_flux_edge (faces of ghost "
+             "cells); GP recon + HLLC + quadrature" if fp == pkg.FP_FAST
+             else "first pass of one RK stage: k_flux_tile x and y (GP recon + HLLC + quadrature)")
     roofline = {"bound": "fp64", "kernel": kname,
                 "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",
                 "frac": achieved_tflops / peak_tflops,

@@ -40,6 +40,8 @@ struct gpmood_batch {
     GridBar* hbar = nullptr;  // pinned
     int4* ftiles[GPM_NTILES] = {};
     int nft[GPM_NTILES] = {};
+    int4* etiles = nullptr;  // edge items of the two-direction cell tiles
+    int net = 0;
     int2* cblocks = nullptr;
     int ncb = 0;
     int2* pblocks = nullptr;
@@ -101,6 +103,8 @@ BatchArgs make_args(gpmood_batch* b, const double* uin, double* uout, int stage)
     a.ntrb = b->ntrb;
     a.ftiles = b->ftiles[b->tile];
     a.nftiles = b->nft[b->tile];
+    a.etiles = b->etiles;
+    a.netiles = b->net;
     a.cblocks = b->cblocks;
     a.ncblocks = b->ncb;
     a.pblocks = b->pblocks;
@@ -179,6 +183,7 @@ void free_batch(gpmood_batch* b) {
     cudaFree(b->order); cudaFree(b->stamp); cudaFree(b->list[0]); cudaFree(b->list[1]);
     cudaFree(b->ntrb); cudaFree(b->bar); cudaFree(b->cblocks); cudaFree(b->pblocks);
     for (int k = 0; k < GPM_NTILES; k++) cudaFree(b->ftiles[k]);
+    cudaFree(b->etiles);
     if (b->hsc) cudaFreeHost(b->hsc);
     if (b->hntrb) cudaFreeHost(b->hntrb);
     if (b->hbar) cudaFreeHost(b->hbar);
@@ -255,9 +260,13 @@ int gpmood_batch_create(const gpmood_params* p, int nprob, const int* lf, const 
         return (long long)lf[x] * nf[x] > (long long)lf[y] * nf[y];
     });
     std::vector<int4> ft[GPM_NTILES];
-    for (int i : ord)  // two-direction cell tiles over [0,lf] x [0,nf]
-        for (int n0 = 0; n0 <= nf[i]; n0 += kTileTY[GPM_TILE_XY])
-            for (int l0 = 0; l0 <= lf[i]; l0 += kTileTX[GPM_TILE_XY]) ft[GPM_TILE_XY].push_back(make_int4(i, 2, l0, n0));
+    std::vector<int4> et;  // edge items of the two-direction cell tiles
+    for (int i : ord) {  // two-direction cell tiles over the interior, and 256-face edge items
+        for (int n0 = 1; n0 <= nf[i]; n0 += kTileTY[GPM_TILE_XY])
+            for (int l0 = 1; l0 <= lf[i]; l0 += kTileTX[GPM_TILE_XY]) ft[GPM_TILE_XY].push_back(make_int4(i, 2, l0, n0));
+        for (int k0 = 0; k0 < lf[i] + nf[i]; k0 += kTileTX[GPM_TILE_XY] * kTileTY[GPM_TILE_XY])
+            et.push_back(make_int4(i, 3, k0, 0));
+    }
     for (int k = 0; k < GPM_NTILES; k++) {
         if (k == GPM_TILE_XY) continue;
         for (int i : ord) {
@@ -307,6 +316,8 @@ int gpmood_batch_create(const gpmood_params* p, int nprob, const int* lf, const 
         BALLOC(b->ftiles[k], sizeof(int4) * ft[k].size());
         b->nft[k] = (int)ft[k].size();
     }
+    BALLOC(b->etiles, sizeof(int4) * et.size());
+    b->net = (int)et.size();
 #undef BALLOC
     if (cudaMallocHost((void**)&b->hsc, sizeof(BScal) * nprob) != cudaSuccess ||
         cudaMallocHost((void**)&b->hntrb, 8 * sizeof(int)) != cudaSuccess ||
@@ -332,6 +343,7 @@ int gpmood_batch_create(const gpmood_params* p, int nprob, const int* lf, const 
               cudaMemcpyAsync(b->pblocks, pb.data(), sizeof(int2) * pb.size(), cudaMemcpyHostToDevice, s) == cudaSuccess;
     for (int k = 0; ok && k < GPM_NTILES; k++)
         ok = cudaMemcpyAsync(b->ftiles[k], ft[k].data(), sizeof(int4) * ft[k].size(), cudaMemcpyHostToDevice, s) == cudaSuccess;
+    ok = ok && cudaMemcpyAsync(b->etiles, et.data(), sizeof(int4) * et.size(), cudaMemcpyHostToDevice, s) == cudaSuccess;
     ok = ok && cudaMemsetAsync(b->U, 0, sb, s) == cudaSuccess && cudaMemsetAsync(b->Ur, 0, sb, s) == cudaSuccess &&
          cudaMemsetAsync(b->U1, 0, sb, s) == cudaSuccess && cudaMemsetAsync(b->U2, 0, sb, s) == cudaSuccess &&
          cudaMemsetAsync(b->Fx, 0, sb, s) == cudaSuccess && cudaMemsetAsync(b->Fy, 0, sb, s) == cudaSuccess &&

@@ -42,6 +42,8 @@ struct BatchArgs {
     int* ntrb;            // [0..1] list counts, [2] pass epoch, [3] cap flag, [4] detected, [5] passes
     const int4* ftiles;
     int nftiles;
+    const int4* etiles;   // edge items of the two-direction cell tiles
+    int netiles;
     const int2* cblocks;
     int ncblocks;
     const int2* pblocks;
@@ -52,7 +54,9 @@ struct BatchArgs {
 
 // Face-tile shapes (TX x TY faces per CTA) the autotuner chooses from.  The
 // last one is the fast mode's two-direction cell tile (order 5, ngp = 3
-// only): items (problem, 2, l0, n0) over cells [0,lf] x [0,nf].
+// only): items (problem, 2, l0, n0) over the interior cells, with edge items
+// (problem, 3, k0, 0) in BatchArgs::etiles for the faces whose low cell is a
+// ghost.
 #define GPM_NTILES 5
 #define GPM_TILE_XY 4
 static const int kTileTX[GPM_NTILES] = {32, 32, 16, 64, 32};

@@ -202,6 +202,10 @@ __global__ void __launch_bounds__(TX * TY) k_flux_tile(StageArgs a, const __grid
     st_cell(out, Cell{F[0], F[1], F[2], F[3]});
 }
 
+template <int DIR, int NP, int NGP>
+__device__ __forceinline__ void face_global(const GridGeom& g, const GpWeights& w, int o, const double* __restrict__ uin,
+                                            size_t c0, double* F);
+
 #if !GPM_EXACT
 // ---------------------------------------------------------------------------
 // Fast first pass at uniform order 5 with ngp = 3: both face directions of a
@@ -213,9 +217,10 @@ __global__ void __launch_bounds__(TX * TY) k_flux_tile(StageArgs a, const __grid
 // on its own.  A cell keeps its right and top states in registers and passes
 // its left and bottom states to its neighbours through shared memory; then
 // every thread solves the x face and the y face of which its cell is the low
-// side.  The tile owns cells (l0..l0+XT-1, n0..n0+XY-1) of l in [0,lf],
-// n in [0,nf]; one extra column (left states) and row (bottom states) is
-// computed by two warps.
+// side.  Tiles own the interior cells (l0..l0+XT-1, n0..n0+XY-1), l0, n0 >= 1;
+// one extra column (left states) and row (bottom states) is computed by two
+// warps.  The faces whose low cell is a ghost -- x faces (0,n), y faces (l,0)
+// -- are 256-face edge items computed face by face (edge_faces).
 constexpr int XT = 32, XY = 8;          // cells per tile
 constexpr int XS = 13;                  // doubles per published state set (12 used, padded)
 
@@ -350,7 +355,7 @@ __device__ __forceinline__ void xy_tile(const GridGeom& g, const GpWeights& w, c
         publish(sm.left[tx][XT - 1], e.lo);
     }
     __syncthreads();
-    if (l <= g.lf && n >= 1 && n <= g.nf) {  // x face between (l,n) and (l+1,n)
+    if (l <= g.lf && n <= g.nf) {  // x face between (l,n) and (l+1,n)
         double uR[3][4], F[4];
         const double* src = sm.left[ty][tx];
 #pragma unroll
@@ -360,7 +365,7 @@ __device__ __forceinline__ void xy_tile(const GridGeom& g, const GpWeights& w, c
         quad_flux<0, 3>(xs.hi, uR, w.gw, F);
         st_cell(fx + 4 * cidx(g, l, n), Cell{F[0], F[1], F[2], F[3]});
     }
-    if (l >= 1 && l <= g.lf && n <= g.nf) {  // y face between (l,n) and (l,n+1)
+    if (l <= g.lf && n <= g.nf) {  // y face between (l,n) and (l,n+1)
         double uR[3][4], F[4];
         const double* src = sm.bottom[ty][tx];
 #pragma unroll
@@ -372,10 +377,33 @@ __device__ __forceinline__ void xy_tile(const GridGeom& g, const GpWeights& w, c
     }
 }
 
-__global__ void __launch_bounds__(XT * XY) k_flux_xy(StageArgs a, const __grid_constant__ GpWeights w) {
+// Edge item: faces k0 .. k0+255 of the list [x faces (0,1..nf), y faces (1..lf,0)].
+__device__ __forceinline__ void edge_faces(const GridGeom& g, const GpWeights& w, const double* __restrict__ uin,
+                                           double* __restrict__ fx, double* __restrict__ fy, int k0) {
+    const int k = k0 + threadIdx.y * XT + threadIdx.x;
+    double F[4];
+    if (k < g.nf) {
+        const size_t c0 = cidx(g, 0, k + 1);
+        face_global<0, 13, 3>(g, w, 2, uin, c0, F);
+        st_cell(fx + 4 * c0, Cell{F[0], F[1], F[2], F[3]});
+    } else if (k < g.nf + g.lf) {
+        const size_t c0 = cidx(g, k - g.nf + 1, 0);
+        face_global<1, 13, 3>(g, w, 2, uin, c0, F);
+        st_cell(fy + 4 * c0, Cell{F[0], F[1], F[2], F[3]});
+    }
+}
+
+// One cell tile per block (x fastest).
+__global__ void __launch_bounds__(XT * XY, 2) k_flux_xy(StageArgs a, const __grid_constant__ GpWeights w, int tiles_x) {
     extern __shared__ __align__(16) unsigned char xy_raw[];
     XySmem& sm = *reinterpret_cast<XySmem*>(xy_raw);
-    xy_tile(a.g, w, a.uin, a.fx, a.fy, blockIdx.x * XT, blockIdx.y * XY, sm);
+    const int by = blockIdx.x / tiles_x, bx = blockIdx.x - by * tiles_x;
+    xy_tile(a.g, w, a.uin, a.fx, a.fy, 1 + bx * XT, 1 + by * XY, sm);
+}
+
+// The faces whose low cell is a ghost, 256 per block.
+__global__ void __launch_bounds__(XT * XY) k_flux_edge(StageArgs a, const __grid_constant__ GpWeights w) {
+    edge_faces(a.g, w, a.uin, a.fx, a.fy, blockIdx.x * XT * XY);
 }
 
 bool launch_flux_xy(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
@@ -384,8 +412,10 @@ bool launch_flux_xy(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
         cudaFuncSetAttribute(k_flux_xy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(XySmem));
         attr = true;
     }
-    const dim3 grid((a.g.lf + 1 + XT - 1) / XT, (a.g.nf + 1 + XY - 1) / XY), blk(XT, XY);
-    k_flux_xy<<<grid, blk, sizeof(XySmem), s>>>(a, w);
+    const int tx = (a.g.lf + XT - 1) / XT, ty = (a.g.nf + XY - 1) / XY;
+    const int edges = (a.g.lf + a.g.nf + XT * XY - 1) / (XT * XY);
+    k_flux_xy<<<tx * ty, dim3(XT, XY), sizeof(XySmem), s>>>(a, w, tx);
+    k_flux_edge<<<edges, dim3(XT, XY), 0, s>>>(a, w);
     return true;
 }
 #endif
@@ -409,7 +439,7 @@ void launch_flux_ngp(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
 
 int launch_flux_all(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
 #if !GPM_EXACT
-    if (a.uniform_order && a.g.mord == 5 && a.g.ngp == 3 && launch_flux_xy(a, w, s)) return 1;
+    if (a.uniform_order && a.g.mord == 5 && a.g.ngp == 3 && launch_flux_xy(a, w, s)) return 2;
 #endif
     switch (a.g.ngp) {
     case 1: launch_flux_ngp<1>(a, w, s); break;
@@ -974,7 +1004,7 @@ __global__ void __launch_bounds__(TXB* TYB) kb_flux(BatchArgs a) {
 
 #if !GPM_EXACT
 // The two-direction cell tiles of every problem (xy_tile), persistent CTAs.
-__global__ void __launch_bounds__(XT * XY) kb_flux_xy(BatchArgs a) {
+__global__ void __launch_bounds__(XT * XY, 2) kb_flux_xy(BatchArgs a) {
     extern __shared__ __align__(16) unsigned char xy_raw[];
     XySmem& sm = *reinterpret_cast<XySmem*>(xy_raw);
     for (int item = blockIdx.x; item < a.nftiles; item += gridDim.x) {
@@ -982,6 +1012,15 @@ __global__ void __launch_bounds__(XT * XY) kb_flux_xy(BatchArgs a) {
         const BProb P = a.prob[it.x];
         __syncthreads();  // the previous tile is done with the shared buffers
         xy_tile(bgeom(a, P), a.wtab[P.wc], a.uin + 4 * P.off, a.fx + 4 * P.off, a.fy + 4 * P.off, it.z, it.w, sm);
+    }
+}
+
+// The edge items (problem, 3, k0, 0) of every problem.
+__global__ void __launch_bounds__(XT * XY) kb_flux_edge(BatchArgs a) {
+    for (int item = blockIdx.x; item < a.netiles; item += gridDim.x) {
+        const int4 it = a.etiles[item];
+        const BProb P = a.prob[it.x];
+        edge_faces(bgeom(a, P), a.wtab[P.wc], a.uin + 4 * P.off, a.fx + 4 * P.off, a.fy + 4 * P.off, it.z);
     }
 }
 #endif
@@ -1016,6 +1055,8 @@ static void blaunch_flux_n(const BatchArgs& a, cudaStream_t s) {
         }
         const int grid = a.nftiles < sm_count() * 2 ? a.nftiles : sm_count() * 2;
         kb_flux_xy<<<grid, dim3(XT, XY), sizeof(XySmem), s>>>(a);
+        const int ge = a.netiles < sm_count() * 4 ? a.netiles : sm_count() * 4;
+        if (ge > 0) kb_flux_edge<<<ge, dim3(XT, XY), 0, s>>>(a);
         return;
     }
 #endif

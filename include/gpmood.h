@@ -95,9 +95,9 @@ typedef struct gpmood_counters {
 
 /* Per-kernel device time gathered with CUDA events when timing is on. */
 typedef struct gpmood_timing {
-    double flux_ms;          /* first-pass face kernels (GP recon + HLLC), all launches */
-    long long flux_launches;
-    long long flux_faces;    /* faces computed by those launches */
+    double flux_ms;          /* first-pass face kernels (GP recon + HLLC), all stages */
+    long long flux_launches; /* first passes timed: one per RK stage (its face kernels) */
+    long long flux_faces;    /* faces computed by those passes */
     double update_ms;        /* flux-difference update + DETECTION kernels */
     long long update_launches;
     double mood_ms;          /* MOOD passes 2, 3, ... (mark + faces + cells) */
