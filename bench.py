@@ -169,8 +169,8 @@ def measured_peaks():
 
 
 def ncu_traffic_per_face():
-    """DRAM bytes per face of the first-pass face kernel from the committed ncu summary."""
-    f = ROOT / "profiles" / "ncu_flux_tile_sedov.md"
+    """DRAM bytes per face of the fast first-pass face kernel from the committed ncu summary."""
+    f = ROOT / "profiles" / "ncu_flux_sedov2048.md"
     try:
         m = re.search(r"dram_bytes_per_face:\s*([0-9.eE+-]+)", f.read_text())
         return float(m.group(1)) if m else None
@@ -470,7 +470,7 @@ def run_ours(args, ws, rank, local):
     faces_per_launch = tm.flux_faces / max(tm.flux_launches, 1)
     achieved_tflops = FLOPS_PER_FACE * faces_per_launch / (launch_ms * 1e-3) / 1e12
     peak_tflops = peak_fp64_gflops / 1e3
-    tpf = ncu_traffic_per_face()
+    tpf = ncu_traffic_per_face() if fp == pkg.FP_FAST else None  # the committed capture is of the fast kernel
     kname = ("first pass of one RK stage: k_flux_xy (interior, both directions) + k_flux_edge (faces of ghost "
              "cells); GP recon + HLLC + quadrature" if fp == pkg.FP_FAST
              else "first pass of one RK stage: k_flux_tile x and y (GP recon + HLLC + quadrature)")

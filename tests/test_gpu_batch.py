@@ -1,5 +1,6 @@
 """Batched stepping of many problems of uneven size (gpmood_batch_*): every
-problem of a batch must evolve exactly as it does alone in its own context."""
+problem of a batch must evolve exactly as it does alone in its own context
+(bit for bit in the exact mode; to rounding in the fast mode)."""
 from __future__ import annotations
 
 import numpy as np
@@ -39,7 +40,15 @@ def test_batch_equals_single_problem_runs(pkg, fp_mode):
             Us, ts, _ = s.get_state()
         Ub, tb = got[i]
         assert tb == ts, (i, tb, ts)
-        assert np.array_equal(Ub[4:-4, 4:-4], Us[4:-4, 4:-4]), (i, np.abs(Ub - Us).max())
+        I = (slice(4, -4), slice(4, -4))
+        if fp_mode == 0:
+            assert np.array_equal(Ub[I], Us[I]), (i, np.abs(Ub - Us).max())
+        else:
+            # FMA contraction is the compiler's choice per kernel, so the
+            # batched and single-problem kernels may round differently
+            for k in range(4):
+                rel = np.abs(Ub[I + (k,)] - Us[I + (k,)]).sum() / np.abs(Us[I + (k,)]).sum()
+                assert rel <= 1e-13, (i, k, rel)
 
 
 def test_autotune_keeps_results(pkg):
