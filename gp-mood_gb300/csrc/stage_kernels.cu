@@ -505,6 +505,15 @@ __device__ __forceinline__ int face_item(int i, int nt, int* dir, int* side) {
     return j >> 1;
 }
 
+// The order cascade of a troubled cell, mod_subroutine_MOOD.f90:159-163
+// (5 -> 3, 3 -> 1).  It is applied by the thread that finds the cell troubled,
+// when it lists the cell: no other thread reads that cell's order before the
+// next pass's faces, which come after a grid barrier or a kernel boundary.
+__device__ __forceinline__ void cascade_order(int8_t* o) {
+    const int v = *o;
+    *o = (int8_t)(v == 3 ? 1 : (v > 3 ? 3 : v));
+}
+
 __global__ void __launch_bounds__(256) k_update_detect(StageArgs a, const __grid_constant__ GpWeights w, int cur) {
     const GridGeom& g = a.g;
     const int l = 1 + blockIdx.x * 32 + threadIdx.x, n = 1 + blockIdx.y * 8 + threadIdx.y;
@@ -518,6 +527,7 @@ __global__ void __launch_bounds__(256) k_update_detect(StageArgs a, const __grid
         const int o = a.uniform_order ? g.mord : (int)a.order[c];
         if (o > 1) trb = mood_troubled(uo, a.uin + 4 * c, g.nx, g, w.d2x, w.d2y);
     }
+    if (trb) cascade_order(&a.order[c]);
     list_append(trb, a.tlist[cur], &a.sc->ntrb[cur], (int)c);
 }
 
@@ -531,13 +541,10 @@ void launch_update_detect(const StageArgs& a, const GpWeights& w, int cur, cudaS
 
 constexpr int LIST_CTAS_PER_SM = 4;
 
+// Start of a host-driven MOOD pass: count the listed cells (their orders
+// were lowered when they were listed) and empty the next list.
 __global__ void k_mood_mark(StageArgs a, int cur) {
     const int nt = a.sc->ntrb[cur];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
-        const int c = a.tlist[cur][i];
-        const int o = a.order[c];
-        a.order[c] = (int8_t)(o == 3 ? 1 : (o > 3 ? 3 : o));  // mod_subroutine_MOOD.f90:159-163
-    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         atomicAdd(&a.sc->detected_step, (unsigned long long)nt);
         a.sc->ntrb[cur ^ 1] = 0;
@@ -622,6 +629,7 @@ __global__ void __launch_bounds__(256) k_mood_cells(StageArgs a, const __grid_co
                 cval = (int)c;
             }
         }
+        if (trb) cascade_order(&a.order[cval]);
         list_append(trb, a.tlist[nxt], &a.sc->ntrb[nxt], cval);
     }
 }
@@ -633,6 +641,10 @@ __global__ void __launch_bounds__(256) k_mood_cells(StageArgs a, const __grid_co
 // (cooperative launch), so the barrier cannot wait on an unscheduled CTA; its
 // spin is still bounded, and a timeout records GPM_STATUS_BARRIER and makes
 // every CTA leave.
+
+// Threads per CTA of the cooperative MOOD loops: one 16-warp CTA per SM
+// keeps the barrier's arrival count at the SM count.
+constexpr int MOOD_THREADS = 512;
 
 __device__ __forceinline__ bool grid_sync(GridBar* b) {
     __syncthreads();
@@ -661,7 +673,7 @@ __device__ __forceinline__ bool grid_sync(GridBar* b) {
 }
 
 template <int NGP>
-__global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_constant__ GpWeights w, GridBar* bar,
+__global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, const __grid_constant__ GpWeights w, GridBar* bar,
                                                       int max_pass, int stage) {
     const GridGeom& g = a.g;
     const double qx = a.sc->qx, qy = a.sc->qy;
@@ -677,17 +689,11 @@ __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_
             break;
         }
         pass++;
-        // cascade of the troubled cells' orders, mod_subroutine_MOOD.f90:159-163
-        for (int i = stid; i < nt; i += gstride) {
-            const int c = a.tlist[cur][i];
-            const int o = a.order[c];
-            a.order[c] = (int8_t)(o == 3 ? 1 : (o > 3 ? 3 : o));
-        }
+        // the listed cells' orders were lowered when they were listed
         if (gtid == 0) {
-            a.sc->ntrb[cur ^ 1] = 0;
+            a.sc->ntrb[cur ^ 1] = 0;  // nobody appends to it before the next barrier
             a.sc->detected_step += (unsigned long long)nt;
         }
-        if (!grid_sync(bar)) return;
         // the four faces of every troubled cell at the new orders
         for (int i = stid; i < 4 * nt; i += gstride) {
             int dir, side;
@@ -716,6 +722,7 @@ __global__ void __launch_bounds__(256, 1) k_mood_loop(StageArgs a, const __grid_
                     cval = (int)c;
                 }
             }
+            if (trb) cascade_order(&a.order[cval]);
             list_append(trb, a.tlist[nxt], &a.sc->ntrb[nxt], cval);
         }
         if (!grid_sync(bar)) return;
@@ -735,13 +742,13 @@ static int launch_mood_loop_n(const StageArgs& a, const GpWeights& w, GridBar* b
         int dev = 0, sms = 0, occ = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mood_loop<NGP>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mood_loop<NGP>, MOOD_THREADS, 0);
         grid = sms * (occ > 0 ? occ : 1);
     }
     StageArgs aa = a;
     GpWeights ww = w;
     void* args[] = {&aa, &ww, &bar, &max_pass, &stage};
-    return cudaLaunchCooperativeKernel((const void*)k_mood_loop<NGP>, dim3(grid), dim3(256), args, 0, s) == cudaSuccess
+    return cudaLaunchCooperativeKernel((const void*)k_mood_loop<NGP>, dim3(grid), dim3(MOOD_THREADS), args, 0, s) == cudaSuccess
                ? 0
                : -1;
 }
@@ -1109,6 +1116,7 @@ __global__ void __launch_bounds__(256) kb_update(BatchArgs a) {
                 trb = mood_troubled(uo, ub + 4 * c, g.nx, g, a.wtab[P.wc].d2x, a.wtab[P.wc].d2y);
             cl = (int)c;
         }
+        if (trb) cascade_order(a.order + P.off + cl);
         list_append2(trb, a.tlist[0], &a.ntrb[0], make_int2(it.x, cl));
     }
 }
@@ -1121,15 +1129,9 @@ void blaunch_update(const BatchArgs& a, cudaStream_t s) {
 // One MOOD pass over every problem's list: cascade, the troubled cells' faces,
 // then their 5-point crosses.  Each kernel returns at once on an empty list,
 // so a captured graph holds a fixed number of passes at almost no cost.
-__global__ void kb_mood_mark(BatchArgs a, int cur) {
+__global__ void kb_mood_mark(BatchArgs a, int cur) {  // the listed cells' orders are already lowered
     const int nt = a.ntrb[cur];
     if (nt == 0) return;
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < nt; i += gridDim.x * blockDim.x) {
-        const int2 e = a.tlist[cur][i];
-        int8_t* o = a.order + a.prob[e.x].off + e.y;
-        const int v = *o;
-        *o = (int8_t)(v == 3 ? 1 : (v > 3 ? 3 : v));
-    }
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.ntrb[cur ^ 1] = 0;
         a.ntrb[2] += 1;  // pass epoch for the de-duplication stamps
@@ -1187,6 +1189,7 @@ __global__ void __launch_bounds__(256) kb_mood_cells(BatchArgs a, int cur) {
                 val = make_int2(e.x, (int)c);
             }
         }
+        if (trb) cascade_order(a.order + a.prob[val.x].off + val.y);
         list_append2(trb, a.tlist[nxt], &a.ntrb[nxt], val);
     }
 }
@@ -1208,7 +1211,7 @@ void blaunch_mood_pass(const BatchArgs& a, int cur, cudaStream_t s) {
 // passes run until every problem's list is empty.  ntrb[2] is the stamp epoch,
 // ntrb[4] the detected-cell total, ntrb[5] the pass count of the last stage.
 template <int NGP>
-__global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar, int max_pass) {
+__global__ void __launch_bounds__(MOOD_THREADS, 1) kb_mood_loop(BatchArgs a, GridBar* bar, int max_pass) {
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     const int stid = pack_tid();
     int cur = 0, pass = 1;
@@ -1220,18 +1223,12 @@ __global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar
             break;
         }
         pass++;
-        for (int i = stid; i < nt; i += gstride) {
-            const int2 e = a.tlist[cur][i];
-            int8_t* o = a.order + a.prob[e.x].off + e.y;
-            const int v = *o;
-            *o = (int8_t)(v == 3 ? 1 : (v > 3 ? 3 : v));
-        }
+        // the listed cells' orders were lowered when they were listed
         if (gtid == 0) {
-            a.ntrb[cur ^ 1] = 0;
-            a.ntrb[2] += 1;
+            a.ntrb[cur ^ 1] = 0;  // nobody appends to it before the next barrier
+            a.ntrb[2] += 1;       // stamp epoch, read after the next barrier
             a.ntrb[4] += nt;
         }
-        if (!grid_sync(bar)) return;
         for (int i = stid; i < 4 * nt; i += gstride) {
             int dir, side;
             const int2 e = a.tlist[cur][face_item(i, nt, &dir, &side)];
@@ -1274,6 +1271,7 @@ __global__ void __launch_bounds__(256, 1) kb_mood_loop(BatchArgs a, GridBar* bar
                     val = make_int2(e.x, (int)c);
                 }
             }
+            if (trb) cascade_order(a.order + a.prob[val.x].off + val.y);
             list_append2(trb, a.tlist[nxt], &a.ntrb[nxt], val);
         }
         if (!grid_sync(bar)) return;
@@ -1287,12 +1285,12 @@ static int blaunch_mood_loop_n(const BatchArgs& a, GridBar* bar, int max_pass, c
     static int grid = 0;
     if (!grid) {
         int occ = 0;
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kb_mood_loop<NGP>, 256, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kb_mood_loop<NGP>, MOOD_THREADS, 0);
         grid = sm_count() * (occ > 0 ? occ : 1);
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);
-    cfg.blockDim = dim3(256);
+    cfg.blockDim = dim3(MOOD_THREADS);
     cfg.stream = s;
     cudaLaunchAttribute attr;
     attr.id = cudaLaunchAttributeCooperative;
