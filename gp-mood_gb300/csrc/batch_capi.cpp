@@ -261,10 +261,10 @@ int gpmood_batch_create(const gpmood_params* p, int nprob, const int* lf, const 
     });
     std::vector<int4> ft[GPM_NTILES];
     std::vector<int4> et;  // edge items of the two-direction cell tiles
-    for (int i : ord) {  // two-direction cell tiles over the interior, and 256-face edge items
+    for (int i : ord) {  // two-direction cell tiles over the interior, and 32-face edge items
         for (int n0 = 1; n0 <= nf[i]; n0 += kTileTY[GPM_TILE_XY])
             for (int l0 = 1; l0 <= lf[i]; l0 += kTileTX[GPM_TILE_XY]) ft[GPM_TILE_XY].push_back(make_int4(i, 2, l0, n0));
-        for (int k0 = 0; k0 < lf[i] + nf[i]; k0 += kTileTX[GPM_TILE_XY] * kTileTY[GPM_TILE_XY])
+        for (int k0 = 0; k0 < lf[i] + nf[i]; k0 += 32)  // one warp of edge faces per item
             et.push_back(make_int4(i, 3, k0, 0));
     }
     for (int k = 0; k < GPM_NTILES; k++) {

@@ -55,6 +55,7 @@ struct gpmood_ctx {
 };
 
 double gpm_probe_fp64();
+int gpm_fast_rcp_dev(const double* x, double* y, int n);
 
 namespace {
 
@@ -621,6 +622,12 @@ int gpmood_probe_fp64(double* gflops) {
     const double g = gpm_probe_fp64();
     if (!(g > 0)) return fail(nullptr, GPMOOD_E_CUDA, "FP64 probe failed: %s", cudaGetErrorString(cudaGetLastError()));
     *gflops = g;
+    return 0;
+}
+
+int gpmood_fast_rcp(const double* d_x, double* d_y, int n) {
+    if ((!d_x || !d_y) && n > 0) return fail(nullptr, GPMOOD_E_ARG, "NULL argument");
+    if (gpm_fast_rcp_dev(d_x, d_y, n)) return fail(nullptr, GPMOOD_E_CUDA, "fast_rcp: %s", cudaGetErrorString(cudaGetLastError()));
     return 0;
 }
 

@@ -8,6 +8,7 @@
 // mod_HLLC.f90:11-169 (HLLC_Flux), mod_GP_MOOD.f90:58-65 (dot products),
 // mod_subroutine_MOOD.f90:41-131,191-238 (DETECTION checks, shock_detector).
 #pragma once
+#include "fast_rcp.cuh"
 #include "gpm_common.h"
 
 #ifndef GPM_EXACT
@@ -189,7 +190,7 @@ __device__ __forceinline__ void hllc(const double* ul, const double* ur, double*
     const Prim L = c2p<DIR>(ul);
     const Prim R = c2p<DIR>(ur);
 #else
-    const double rr = 1.0 / (ul[0] * ur[0]);  // one division for both 1/rho
+    const double rr = gpm_fast_rcp(ul[0] * ur[0]);  // one reciprocal for both 1/rho
     const Prim L = c2p<DIR>(ul, ur[0] * rr);
     const Prim R = c2p<DIR>(ur, ul[0] * rr);
 #endif
@@ -208,7 +209,11 @@ __device__ __forceinline__ void hllc(const double* ul, const double* ur, double*
     double uStar = ul[0] * L.vn * numerL - ur[0] * R.vn * numerR;
     uStar = (R.p - L.p) + uStar;
     const double aL = ul[0] * numerL, aR = ur[0] * numerR;
+#if GPM_EXACT
     uStar = uStar / (aL - aR);
+#else
+    uStar = uStar * gpm_fast_rcp(aL - aR);
+#endif
     const bool left = (SL < 0.) && (uStar >= 0.);
     const bool right = (uStar < 0.) && (SR >= 0.);
     if (!left && !right) {
@@ -230,7 +235,7 @@ __device__ __forceinline__ void hllc(const double* ul, const double* ur, double*
     st[3] = u[3] / u[0] + (uStar - s.vn) * (uStar + s.p / a);
 #else
     const double den = S - uStar;
-    const double inv = 1.0 / (a * den);  // one division for a/den and p/a
+    const double inv = gpm_fast_rcp(a * den);  // one reciprocal for a/den and p/a
     const double dStar = a * a * inv;
     st[3] = u[3] * s.ir + (uStar - s.vn) * (uStar + s.p * den * inv);
 #endif

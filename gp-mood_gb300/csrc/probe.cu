@@ -1,8 +1,11 @@
-// probe.cu -- FP64 FMA throughput microbenchmark (roofline denominator).
+// probe.cu -- FP64 FMA throughput microbenchmark (roofline denominator), and
+// the fast mode's reciprocal on caller arrays (for its accuracy test).
 //
 // Every thread runs 8 independent FMA chains; the grid covers every SM several
 // times over, so the FP64 pipe, not latency, bounds the kernel.
 #include <cuda_runtime.h>
+
+#include "fast_rcp.cuh"
 
 namespace {
 
@@ -16,7 +19,19 @@ __global__ void k_dfma(double* out, int iters, double b, double c) {
     out[blockIdx.x * blockDim.x + threadIdx.x] = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
 }
 
+__global__ void k_fast_rcp(const double* x, double* y, int n) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) y[i] = gpm_fast_rcp(x[i]);
+}
+
 }  // namespace
+
+// y[i] = the fast mode's 1/x[i] for device arrays of n doubles; 0 or -1.
+int gpm_fast_rcp_dev(const double* x, double* y, int n) {
+    if (n <= 0) return 0;
+    k_fast_rcp<<<(n + 255) / 256, 256>>>(x, y, n);
+    return cudaDeviceSynchronize() == cudaSuccess ? 0 : -1;
+}
 
 // Returns GFLOP/s (FMA = 2 flops) of the best of three runs, or a negative value on error.
 double gpm_probe_fp64() {

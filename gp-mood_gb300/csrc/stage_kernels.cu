@@ -220,7 +220,7 @@ __device__ __forceinline__ void face_global(const GridGeom& g, const GpWeights& 
 // side.  Tiles own the interior cells (l0..l0+XT-1, n0..n0+XY-1), l0, n0 >= 1;
 // one extra column (left states) and row (bottom states) is computed by two
 // warps.  The faces whose low cell is a ghost -- x faces (0,n), y faces (l,0)
-// -- are 256-face edge items computed face by face (edge_faces).
+// -- are 32-face edge items computed face by face (edge_faces).
 constexpr int XT = 32, XY = 8;          // cells per tile
 constexpr int XS = 13;                  // doubles per published state set (12 used, padded)
 
@@ -377,10 +377,12 @@ __device__ __forceinline__ void xy_tile(const GridGeom& g, const GpWeights& w, c
     }
 }
 
-// Edge item: faces k0 .. k0+255 of the list [x faces (0,1..nf), y faces (1..lf,0)].
+// Edge item: faces k0 .. k0+EDGE_T-1 of the list [x faces (0,1..nf), y faces
+// (1..lf,0)], one warp per item so that the few edge faces spread over many SMs.
+constexpr int EDGE_T = 32;
 __device__ __forceinline__ void edge_faces(const GridGeom& g, const GpWeights& w, const double* __restrict__ uin,
                                            double* __restrict__ fx, double* __restrict__ fy, int k0) {
-    const int k = k0 + threadIdx.y * XT + threadIdx.x;
+    const int k = k0 + (int)threadIdx.x;
     double F[4];
     if (k < g.nf) {
         const size_t c0 = cidx(g, 0, k + 1);
@@ -401,9 +403,9 @@ __global__ void __launch_bounds__(XT * XY, 2) k_flux_xy(StageArgs a, const __gri
     xy_tile(a.g, w, a.uin, a.fx, a.fy, 1 + bx * XT, 1 + by * XY, sm);
 }
 
-// The faces whose low cell is a ghost, 256 per block.
-__global__ void __launch_bounds__(XT * XY) k_flux_edge(StageArgs a, const __grid_constant__ GpWeights w) {
-    edge_faces(a.g, w, a.uin, a.fx, a.fy, blockIdx.x * XT * XY);
+// The faces whose low cell is a ghost, EDGE_T per block.
+__global__ void __launch_bounds__(EDGE_T) k_flux_edge(StageArgs a, const __grid_constant__ GpWeights w) {
+    edge_faces(a.g, w, a.uin, a.fx, a.fy, blockIdx.x * EDGE_T);
 }
 
 bool launch_flux_xy(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
@@ -413,9 +415,9 @@ bool launch_flux_xy(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
         attr = true;
     }
     const int tx = (a.g.lf + XT - 1) / XT, ty = (a.g.nf + XY - 1) / XY;
-    const int edges = (a.g.lf + a.g.nf + XT * XY - 1) / (XT * XY);
+    const int edges = (a.g.lf + a.g.nf + EDGE_T - 1) / EDGE_T;
     k_flux_xy<<<tx * ty, dim3(XT, XY), sizeof(XySmem), s>>>(a, w, tx);
-    k_flux_edge<<<edges, dim3(XT, XY), 0, s>>>(a, w);
+    k_flux_edge<<<edges, EDGE_T, 0, s>>>(a, w);
     return true;
 }
 #endif
@@ -1023,7 +1025,7 @@ __global__ void __launch_bounds__(XT * XY, 2) kb_flux_xy(BatchArgs a) {
 }
 
 // The edge items (problem, 3, k0, 0) of every problem.
-__global__ void __launch_bounds__(XT * XY) kb_flux_edge(BatchArgs a) {
+__global__ void __launch_bounds__(EDGE_T) kb_flux_edge(BatchArgs a) {
     for (int item = blockIdx.x; item < a.netiles; item += gridDim.x) {
         const int4 it = a.etiles[item];
         const BProb P = a.prob[it.x];
@@ -1062,8 +1064,8 @@ static void blaunch_flux_n(const BatchArgs& a, cudaStream_t s) {
         }
         const int grid = a.nftiles < sm_count() * 2 ? a.nftiles : sm_count() * 2;
         kb_flux_xy<<<grid, dim3(XT, XY), sizeof(XySmem), s>>>(a);
-        const int ge = a.netiles < sm_count() * 4 ? a.netiles : sm_count() * 4;
-        if (ge > 0) kb_flux_edge<<<ge, dim3(XT, XY), 0, s>>>(a);
+        const int ge = a.netiles < sm_count() * 16 ? a.netiles : sm_count() * 16;
+        if (ge > 0) kb_flux_edge<<<ge, EDGE_T, 0, s>>>(a);
         return;
     }
 #endif

@@ -215,6 +215,9 @@ int  gpmood_get_timing(const gpmood_ctx* ctx, gpmood_timing* out);
 /* FP64 FMA throughput of the current GPU in GFLOP/s (2 flops per FMA),
  * from a short dependent-chain microbenchmark; the FP64 roofline denominator. */
 int  gpmood_probe_fp64(double* gflops);
+/* The fast mode's reciprocal (Newton-Raphson from the hardware approximation)
+ * on device arrays: d_y[i] = 1/d_x[i]; for testing its accuracy. */
+int  gpmood_fast_rcp(const double* d_x, double* d_y, int n);
 
 /* ---- a-priori MLP gate (method GPMOOD_NN_GP_MOOD) ---- */
 

@@ -39,11 +39,12 @@ def test_batch_equals_single_problem_runs(pkg, fp_mode):
             assert s.advance(nsteps) == nsteps
             Us, ts, _ = s.get_state()
         Ub, tb = got[i]
-        assert tb == ts, (i, tb, ts)
         I = (slice(4, -4), slice(4, -4))
         if fp_mode == 0:
+            assert tb == ts, (i, tb, ts)
             assert np.array_equal(Ub[I], Us[I]), (i, np.abs(Ub - Us).max())
         else:
+            assert abs(tb - ts) <= 1e-14 * ts, (i, tb, ts)
             # FMA contraction is the compiler's choice per kernel, so the
             # batched and single-problem kernels may round differently
             for k in range(4):
