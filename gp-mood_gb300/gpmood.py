@@ -333,6 +333,27 @@ class Solver:
     def nn_features(self, d_x: int, d_const: int = 0) -> None:
         self._check(self.lib.gpmood_nn_features(self._h, C.c_void_p(d_x), C.c_void_p(d_const or None)))
 
+    def save_snapshot(self, path, problem: str = "", nn_filename: str = "") -> None:
+        """The device-resident state as a snapshot file (snapshot.py; the
+        datasets of the reference's output.f90:77-192)."""
+        from . import snapshot
+        U, t, n = self.get_state()
+        method = {GP_MOOD: "GP_MOOD", GP_SE: "GP_SE", NN_GP_MOOD: "NN_GP_MOOD"}.get(self.p.method, str(self.p.method))
+        snapshot.save_snapshot(path, U, t, n, self.orders(), cfl=self.p.cfl, problem=problem, method=method,
+                               nn_filename=nn_filename)
+
+    def restore(self, path) -> dict:
+        """Restart from a snapshot file (reader.f90:12-120): primitive fields ->
+        conservative state, Boundary_C at the snapshot's time, set_state."""
+        from . import snapshot
+        snap = snapshot.load_snapshot(path)
+        if (int(snap["lf"]), int(snap["nf"])) != (self.lf, self.nf):
+            raise ValueError(f"snapshot is {snap['lf']}x{snap['nf']}, the solver {self.lf}x{self.nf}")
+        U = snapshot.state_from_snapshot(snap)
+        self.Boundary_C(U, float(snap["time"]))
+        self.set_state(U, float(snap["time"]))
+        return snap
+
     def set_state_dev(self, d_u: int, t: float = 0.0) -> None:
         self._check(self.lib.gpmood_set_state_dev(self._h, C.c_void_p(d_u), float(t)))
 
