@@ -9,10 +9,10 @@ Package layout:
   ic.py        initial conditions of the benchmark problems
   build.py     in-tree build of libgpmood.so
 """
-from .gpmood import (DMR, FP_EXACT, FP_FAST, GP_MOOD, GP_SE, HLLC, NEUMANN, NGC, NN_GP_MOOD, PERIODIC,
-                     REFLECTIVE, SSP_RK3, Adjoint, Batch, GpmoodError, Params, Solver, default_params, gp_weights,
-                     load_library, padded, probe_fp64)
+from .gpmood import (DMR, FE, FP_EXACT, FP_FAST, GP_MOOD, GP_SE, HLL, HLLC, LLF, NEUMANN, NGC, NN_GP_MOOD,
+                     PERIODIC, REFLECTIVE, SSP_RK2, SSP_RK3, SSP_RK4, UNSPLIT, Adjoint, Batch, GpmoodError, Params,
+                     Solver, default_params, gp_weights, load_library, padded, probe_fp64)
 
-__all__ = ["DMR", "FP_EXACT", "FP_FAST", "GP_MOOD", "GP_SE", "HLLC", "NEUMANN", "NGC", "NN_GP_MOOD", "PERIODIC",
-           "REFLECTIVE", "SSP_RK3", "Adjoint", "Batch", "GpmoodError", "Params", "Solver", "default_params",
-           "gp_weights", "load_library", "padded", "probe_fp64"]
+__all__ = ["DMR", "FE", "FP_EXACT", "FP_FAST", "GP_MOOD", "GP_SE", "HLL", "HLLC", "LLF", "NEUMANN", "NGC",
+           "NN_GP_MOOD", "PERIODIC", "REFLECTIVE", "SSP_RK2", "SSP_RK3", "SSP_RK4", "UNSPLIT", "Adjoint", "Batch",
+           "GpmoodError", "Params", "Solver", "default_params", "gp_weights", "load_library", "padded", "probe_fp64"]

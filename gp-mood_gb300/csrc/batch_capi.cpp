@@ -92,6 +92,7 @@ BatchArgs make_args(gpmood_batch* b, const double* uin, double* uout, int stage)
     a.dmp = b->p.dmp;
     a.u2 = b->p.u2;
     a.u2_tol = b->p.u2_tol;
+    a.num_flux = b->p.num_flux;
     a.uin = uin;
     a.uout = uout;
     a.fx = b->Fx;
@@ -202,7 +203,8 @@ int gpmood_batch_create(const gpmood_params* p, int nprob, const int* lf, const 
         return bfail(nullptr, GPMOOD_E_ARG, "batched method must be GP_MOOD (2) or GP_SE (202)");
     if (p->bc_type != GPMOOD_NEUMANN && p->bc_type != GPMOOD_PERIODIC && p->bc_type != GPMOOD_REFLECTIVE)
         return bfail(nullptr, GPMOOD_E_ARG, "batched BC_type must be Neumann, periodic or reflective");
-    if (p->integrator != GPMOOD_SSP_RK3 || p->num_flux != GPMOOD_HLLC || !(p->mord == 1 || p->mord == 3 || p->mord == 5) ||
+    if (p->integrator != GPMOOD_SSP_RK3 || p->num_flux < GPMOOD_HLLC || p->num_flux > GPMOOD_UNSPLIT ||
+        !(p->mord == 1 || p->mord == 3 || p->mord == 5) ||
         p->ngp < 1 || p->ngp > 5 || (p->fp_mode != GPMOOD_FP_EXACT && p->fp_mode != GPMOOD_FP_FAST) ||
         p->max_mood_iters < 0 || !(p->cfl > 0) || !(p->lx > 0) || !(p->ly > 0) || !(p->ell_o_dx > 0))
         return bfail(nullptr, GPMOOD_E_ARG, "unsupported batch knobs");
@@ -214,7 +216,7 @@ int gpmood_batch_create(const gpmood_params* p, int nprob, const int* lf, const 
     b->p = *p;
     b->nprob = nprob;
     b->bt = p->fp_mode == GPMOOD_FP_FAST ? &gpm_fast::batch_table : &gpm_exact::batch_table;
-    b->xy_ok = p->fp_mode == GPMOOD_FP_FAST && p->mord == 5 && p->ngp == 3;
+    b->xy_ok = p->fp_mode == GPMOOD_FP_FAST && p->mord == 5 && p->ngp == 3 && p->num_flux == GPMOOD_HLLC;
     b->tile = b->xy_ok ? GPM_TILE_XY : 0;  // the single-problem path's first pass
     b->set_max_nx = p->fp_mode == GPMOOD_FP_FAST ? gpm_fast::batch_set_max_nx : gpm_exact::batch_set_max_nx;
 

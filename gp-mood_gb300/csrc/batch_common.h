@@ -31,7 +31,7 @@ struct BatchArgs {
     const GpWeights* wtab;  // one weight set per distinct grid size (device memory)
     BScal* sc;
     int nprob;
-    int bc_type, ngp, mord, method, dmp, u2, u2_tol;
+    int bc_type, ngp, mord, method, dmp, u2, u2_tol, num_flux;
     const double* uin;
     double* uout;
     double* fx;

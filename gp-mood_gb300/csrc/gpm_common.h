@@ -15,6 +15,7 @@
 
 #define GPM_NGC 4
 #define GPM_MAXGP 5
+#define GPM_MAXST 5  // RK stages of the longest integrator (SSP-RK4: 5 Forward_Euler calls)
 
 // Mirror-symmetric split of the diamond stencil for ngp = 3.  The Gauss
 // points of an x face (iL, iR) lie along y and those of a y face along x; the
@@ -71,7 +72,7 @@ struct GridGeom {
     double dx, dy;
     int bc_type, ngp, mord, method;
     int dmp, u2, u2_tol;
-    int pad;
+    int num_flux;        // 100 HLLC, 101 LLF, 102 HLL, 103 unsplit
 };
 
 // Scalars that stay on the device across a step.
@@ -81,7 +82,7 @@ struct DevScalars {
     unsigned long long dtmin_bits;    // Setdt reduction slot (bits of a positive double)
     int ntrb[2];                      // troubled-cell counts, double-buffered lists
     int status;                       // GPMOOD status bits
-    int passes_stage[3];              // MOOD passes of each RK stage of the last step (device loop)
+    int passes_stage[GPM_MAXST];      // MOOD passes of each RK stage of the last step (device loop)
     unsigned stamp_epoch;             // first unused pass stamp of the device MOOD loop
     unsigned long long detected_step; // count_detected_cell of the current step
     unsigned long long apriori_step;
@@ -129,6 +130,9 @@ struct KernelTable {
     // pass count goes to sc->passes_stage[stage]; returns -1 if the launch failed
     int (*mood_loop)(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, int stage,
                      cudaStream_t s);
+    // y = sum c[i]*x[i], i < n <= 5, left to right; optionally the Setdt reduction of y
+    void (*lincomb)(const GridGeom& g, double* y, int n, const double* const* x, const double* c, int with_cfl,
+                    DevScalars* sc, cudaStream_t s);
 };
 
 namespace gpm_exact { extern const KernelTable table; }

@@ -40,7 +40,9 @@ struct gpmood_ctx {
     bool dt_pending;              // dSc->dtmin_bits holds Setdt of dU
     gpmood_counters ctr;
     NnGate* nn;                   // a-priori gate and training kernels
-    int8_t* dStageOrd;            // CellGPO at the end of each RK stage (3 x ncell)
+    int8_t* dStageOrd;            // CellGPO at the end of each RK stage (GPM_MAXST x ncell)
+    int nstages;                  // Forward_Euler calls per step: FE 1, SSP-RK2 2, SSP-RK3 3, SSP-RK4 5
+    double* dRk4[5];              // SSP-RK4 work arrays U3, U4, FU3, FU4, Fl (U1, U2 are dU1, dU2)
     float *hvX, *hvY;             // attached training-sample buffers (device), or null
     int* hvCount;
     int hvCap;
@@ -48,8 +50,8 @@ struct gpmood_ctx {
     unsigned hvSeed;
     bool timing;                  // per-kernel CUDA-event timing
     bool trace;                   // GPMOOD_TRACE=1: one line per step on stderr
-    cudaEvent_t ev[3][4];         // per RK stage: flux, update, MOOD loop boundaries
-    int flux_nl[3];               // first-pass face launches of each RK stage
+    cudaEvent_t ev[GPM_MAXST][4]; // per RK stage: flux, update, MOOD loop boundaries
+    int flux_nl[GPM_MAXST];       // first-pass face launches of each RK stage
     gpmood_timing tm;
     char err[512];
 };
@@ -102,14 +104,15 @@ StageArgs stage_args(gpmood_ctx* c, const double* uin, double* uout, int stage, 
     return a;
 }
 
-// One Forward_Euler stage (mod_FE.f90:20-190) from uin (device) into uout.
-// Nothing here waits for the GPU: pass counts and status come back once per
-// step (run_step).
-int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage) {
+// One Forward_Euler stage (mod_FE.f90:20-190) from uin (device) into uout;
+// `stage` counts the Forward_Euler calls of the step, bc_stage selects t_rk
+// for time-dependent boundaries (0: t, 1: t+dt, 2: t+dt/2).  Nothing here
+// waits for the GPU: pass counts and status come back once per step.
+int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, int bc_stage) {
     cudaStream_t s = c->stream;
     const KernelTable& kt = *c->kt;
     cudaEvent_t* ev = c->ev[stage];
-    c->kt->bc(c->g, uin, c->dSc, stage, s);  // Boundary_C(Uin), :64
+    c->kt->bc(c->g, uin, c->dSc, bc_stage, s);  // Boundary_C(Uin), :64
     c->ctr.kernel_launches += 2;
     bool uniform = true;
     CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, s));  // CellGPO = mord, :48
@@ -156,26 +159,100 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage) {
             return fail(c, GPMOOD_E_CUDA, "NN harvest: %s", cudaGetErrorString(cudaGetLastError()));
         c->ctr.kernel_launches += 1;
     }
-    kt.bc(c->g, uout, c->dSc, stage, s);  // the last DETECTION's Boundary_C(Uout)
+    kt.bc(c->g, uout, c->dSc, bc_stage, s);  // the last DETECTION's Boundary_C(Uout)
     c->ctr.kernel_launches += 2;
+    if (c->p.integrator == GPMOOD_SSP_RK4) {  // SSP_RK4_ takes the increment, mod_FE.f90:188
+        const double* x[2] = {uout, uin};
+        const double k[2] = {1.0, -1.0};
+        kt.lincomb(c->g, uout, 2, x, k, 0, c->dSc, s);
+        c->ctr.kernel_launches += 1;
+    }
     return check_launch(c, "stage");
 }
 
-// SSP_RK3_ (mod_SSP_RK3.f90:12-39) from u into ur; t, dt, qx, qy already on the
-// device.  with_cfl fuses the next step's Setdt into the final combination.
-// One host synchronisation per step, at its end.
+// SSP_RK4_, mod_SSP_RK4.f90:12-38, with the constants of constants.f90:46-51.
+int run_rk4(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
+    const KernelTable& kt = *c->kt;
+    cudaStream_t s = c->stream;
+    const double c1 = 0.391752226571890, a20 = 0.444370493651235, a21 = 0.555629506348765,
+                 c2 = 0.368410593050371, a30 = 0.620101851488403, a32 = 0.379898148511597,
+                 c3 = 0.251891774271694, a40 = 0.178079954393132, a43 = 0.821920045606868,
+                 c4 = 0.544974750228521, f2 = 0.517231671970585, f3 = 0.096059710526147,
+                 f4 = 0.386708617503269, ff3 = 0.063692468666290, ff4 = 0.226007483236906;
+    double *U1 = c->dU1, *U2 = c->dU2, *U3 = c->dRk4[0], *U4 = c->dRk4[1], *FU3 = c->dRk4[2], *FU4 = c->dRk4[3],
+           *Fl = c->dRk4[4];
+    int rc;
+    if ((rc = run_stage(c, u, Fl, 0, 0))) return rc;
+    {
+        const double* x[2] = {u, Fl};
+        const double k[2] = {1.0, c1};
+        kt.lincomb(c->g, U1, 2, x, k, 0, c->dSc, s);
+    }
+    if ((rc = run_stage(c, U1, Fl, 1, 0))) return rc;
+    {
+        const double* x[3] = {u, U1, Fl};
+        const double k[3] = {a20, a21, c2};
+        kt.lincomb(c->g, U2, 3, x, k, 0, c->dSc, s);
+    }
+    if ((rc = run_stage(c, U2, Fl, 2, 0))) return rc;
+    {
+        const double* x[3] = {u, U2, Fl};
+        const double k[3] = {a30, a32, c3};
+        kt.lincomb(c->g, U3, 3, x, k, 0, c->dSc, s);
+    }
+    if ((rc = run_stage(c, U3, FU3, 3, 0))) return rc;
+    {
+        const double* x[3] = {u, U3, FU3};
+        const double k[3] = {a40, a43, c4};
+        kt.lincomb(c->g, U4, 3, x, k, 0, c->dSc, s);
+    }
+    if ((rc = run_stage(c, U4, FU4, 4, 0))) return rc;
+    {
+        const double* x[5] = {U2, U3, FU3, U4, FU4};
+        const double k[5] = {f2, f3, ff3, f4, ff4};
+        kt.lincomb(c->g, ur, 5, x, k, with_cfl ? 1 : 0, c->dSc, s);
+    }
+    c->ctr.kernel_launches += 5;
+    return check_launch(c, "SSP-RK4 combinations");
+}
+
+// One time_stepping call (time_stepper.f90:12-23) from u into ur with the
+// configured integrator; t, dt, qx, qy already on the device.  with_cfl fuses
+// the next step's Setdt into the final combination.  One host
+// synchronisation per step, at its end.
 int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
     cudaStream_t s = c->stream;
     CU(cudaMemsetAsync(&c->dSc->detected_step, 0, 2 * sizeof(unsigned long long), s));
-    int rc = run_stage(c, u, c->dU1, 0);
-    if (rc) return rc;
-    rc = run_stage(c, c->dU1, c->dU2, 1);
-    if (rc) return rc;
-    c->kt->combine(c->g, u, c->dU2, 0.75, 0.25, 0, c->dSc, s);  // U2 = 0.75 Uin + 0.25 U2
-    c->ctr.kernel_launches += 2;
-    rc = run_stage(c, c->dU2, ur, 2);
-    if (rc) return rc;
-    c->kt->combine(c->g, u, ur, 1. / 3, 2. / 3, with_cfl ? 1 : 0, c->dSc, s);  // Uout = Uin/3 + 2 Uout/3
+    int rc = 0;
+    if (c->p.integrator == GPMOOD_SSP_RK3) {  // SSP_RK3_, mod_SSP_RK3.f90:12-39
+        rc = run_stage(c, u, c->dU1, 0, 0);
+        if (rc) return rc;
+        rc = run_stage(c, c->dU1, c->dU2, 1, 1);
+        if (rc) return rc;
+        c->kt->combine(c->g, u, c->dU2, 0.75, 0.25, 0, c->dSc, s);  // U2 = 0.75 Uin + 0.25 U2
+        c->ctr.kernel_launches += 2;
+        rc = run_stage(c, c->dU2, ur, 2, 2);
+        if (rc) return rc;
+        c->kt->combine(c->g, u, ur, 1. / 3, 2. / 3, with_cfl ? 1 : 0, c->dSc, s);  // Uout = Uin/3 + 2 Uout/3
+    } else if (c->p.integrator == GPMOOD_SSP_RK2) {  // SSP_RK2_, mod_SSP_RK2.f90:12-24 (t_rk = t)
+        rc = run_stage(c, u, c->dU1, 0, 0);
+        if (rc) return rc;
+        rc = run_stage(c, c->dU1, ur, 1, 0);
+        if (rc) return rc;
+        // 0.5*(Uin+Uout): both halvings are exact, so 0.5*Uin + 0.5*Uout rounds the same
+        c->kt->combine(c->g, u, ur, 0.5, 0.5, with_cfl ? 1 : 0, c->dSc, s);
+        c->ctr.kernel_launches += 1;
+    } else if (c->p.integrator == GPMOOD_SSP_RK4) {
+        rc = run_rk4(c, u, ur, with_cfl);
+        if (rc) return rc;
+    } else {  // FE: one Forward_Euler (time_stepper.f90:18)
+        rc = run_stage(c, u, ur, 0, 0);
+        if (rc) return rc;
+        if (with_cfl) {
+            c->kt->cfl(c->g, ur, c->dSc, s);
+            c->ctr.kernel_launches += 1;
+        }
+    }
     rc = check_launch(c, "combine");
     if (rc) return rc;
     CU(cudaMemcpyAsync(c->hSc, c->dSc, sizeof(DevScalars), cudaMemcpyDeviceToHost, s));
@@ -183,7 +260,7 @@ int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
     CU(cudaStreamSynchronize(s));
     const bool mood = c->p.method == GPMOOD_GP_MOOD || c->p.method == GPMOOD_NN_GP_MOOD;
     long long passes = 0;
-    for (int st = 0; st < 3; st++) {
+    for (int st = 0; st < c->nstages; st++) {
         const long long np = mood ? c->hSc->passes_stage[st] : 1;
         passes += np;
         if (np > c->ctr.max_passes_stage) c->ctr.max_passes_stage = np;
@@ -230,10 +307,13 @@ int set_time(gpmood_ctx* c, double t, double dt) {
 
 int validate(const gpmood_params* p, char* why, size_t n) {
     if (!p) { snprintf(why, n, "params is NULL"); return -1; }
-    if (p->integrator != GPMOOD_SSP_RK3) { snprintf(why, n, "integrator %d unsupported (only SSP_RK3=10)", p->integrator); return -1; }
+    if (p->integrator != GPMOOD_FE && p->integrator != GPMOOD_SSP_RK2 && p->integrator != GPMOOD_SSP_RK3 &&
+        p->integrator != GPMOOD_SSP_RK4) {
+        snprintf(why, n, "integrator %d unsupported (FE=8, SSP_RK2=9, SSP_RK3=10, SSP_RK4=12)", p->integrator); return -1; }
     if (p->method != GPMOOD_GP_MOOD && p->method != GPMOOD_GP_SE && p->method != GPMOOD_NN_GP_MOOD) {
         snprintf(why, n, "method %d unsupported (GP_MOOD=2, GP_SE=202, NN_GP_MOOD=203)", p->method); return -1; }
-    if (p->num_flux != GPMOOD_HLLC) { snprintf(why, n, "numFlux %d unsupported (only HLLC=100)", p->num_flux); return -1; }
+    if (p->num_flux < GPMOOD_HLLC || p->num_flux > GPMOOD_UNSPLIT) {
+        snprintf(why, n, "numFlux %d unsupported (HLLC=100, LLF=101, HLL=102, unsplit=103)", p->num_flux); return -1; }
     if (!(p->mord == 1 || p->mord == 3 || p->mord == 5)) { snprintf(why, n, "Mord %d unsupported (1, 3, 5)", p->mord); return -1; }
     if (p->ngp < 1 || p->ngp > 5) { snprintf(why, n, "ngp %d out of 1..5", p->ngp); return -1; }
     if (p->lf < 4 || p->nf < 4 || p->lf > 65536 || p->nf > 65536) { snprintf(why, n, "grid %dx%d out of range", p->lf, p->nf); return -1; }
@@ -250,11 +330,12 @@ void free_all(gpmood_ctx* c) {
     cudaFree(c->dU); cudaFree(c->dUr); cudaFree(c->dU1); cudaFree(c->dU2);
     cudaFree(c->dFx); cudaFree(c->dFy); cudaFree(c->dOrder); cudaFree(c->dStamp);
     cudaFree(c->dList[0]); cudaFree(c->dList[1]); cudaFree(c->dSc); cudaFree(c->dStageOrd); cudaFree(c->dBar);
+    for (int i = 0; i < 5; i++) cudaFree(c->dRk4[i]);
     if (c->hBar) cudaFreeHost(c->hBar);
     if (c->hSc) cudaFreeHost(c->hSc);
     if (c->hCount) cudaFreeHost(c->hCount);
     if (c->nn) nn_gate_destroy(c->nn);
-    for (int st = 0; st < 3; st++)
+    for (int st = 0; st < GPM_MAXST; st++)
         for (int i = 0; i < 4; i++)
             if (c->ev[st][i]) cudaEventDestroy(c->ev[st][i]);
     if (c->stream) cudaStreamDestroy(c->stream);
@@ -309,6 +390,8 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     c->g.ngp = p->ngp;
     c->g.mord = p->mord;
     c->g.method = p->method;
+    c->g.num_flux = p->num_flux;
+    c->nstages = p->integrator == GPMOOD_FE ? 1 : p->integrator == GPMOOD_SSP_RK2 ? 2 : p->integrator == GPMOOD_SSP_RK4 ? 5 : 3;
     c->g.dmp = p->dmp;
     c->g.u2 = p->u2;
     c->g.u2_tol = p->u2_tol;
@@ -350,7 +433,9 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     ALLOC(c->dList[0], c->ncell * sizeof(int));
     ALLOC(c->dList[1], c->ncell * sizeof(int));
     ALLOC(c->dSc, sizeof(DevScalars));
-    ALLOC(c->dStageOrd, 3 * c->ncell);
+    ALLOC(c->dStageOrd, GPM_MAXST * c->ncell);
+    if (p->integrator == GPMOOD_SSP_RK4)
+        for (int i = 0; i < 5; i++) ALLOC(c->dRk4[i], sb);
     ALLOC(c->dBar, sizeof(GridBar));
 #undef ALLOC
     if (cudaMallocHost((void**)&c->hSc, sizeof(DevScalars)) != cudaSuccess ||
@@ -362,7 +447,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
         delete c;
         return GPMOOD_E_CUDA;
     }
-    for (int i = 0; i < 12; i++) {
+    for (int i = 0; i < 4 * GPM_MAXST; i++) {
         if (cudaEventCreate(&c->ev[i / 4][i % 4]) != cudaSuccess) {
             fail(c, GPMOOD_E_CUDA, "event creation failed");
             free_all(c);
@@ -382,7 +467,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
         cudaMemsetAsync(c->dFx, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dFy, 0, sb, s0) != cudaSuccess ||
         cudaMemsetAsync(c->dU, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dUr, 0, sb, s0) != cudaSuccess ||
         cudaMemsetAsync(c->dU1, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dU2, 0, sb, s0) != cudaSuccess ||
-        cudaMemsetAsync(c->dStageOrd, p->mord, 3 * c->ncell, s0) != cudaSuccess ||
+        cudaMemsetAsync(c->dStageOrd, p->mord, GPM_MAXST * c->ncell, s0) != cudaSuccess ||
         cudaMemsetAsync(c->dBar, 0, sizeof(GridBar), s0) != cudaSuccess ||
         cudaStreamSynchronize(s0) != cudaSuccess) {
         fail(c, GPMOOD_E_CUDA, "device initialisation failed");
@@ -668,7 +753,7 @@ int gpmood_nn_predict(gpmood_ctx* c, signed char* gated, long long* n_gated) {
 
 int gpmood_get_stage_orders(gpmood_ctx* c, int stage, signed char* orders) {
     if (!c || !orders) return fail(c, GPMOOD_E_ARG, "NULL argument");
-    if (stage < 0 || stage > 2) return fail(c, GPMOOD_E_ARG, "stage must be 0, 1 or 2");
+    if (stage < 0 || stage >= c->nstages) return fail(c, GPMOOD_E_ARG, "stage must be in 0..%d", c->nstages - 1);
     CU(cudaMemcpy2DAsync(orders, (size_t)c->p.lf,
                          c->dStageOrd + (size_t)stage * c->ncell + (size_t)GPM_NGC * c->g.nx + GPM_NGC,
                          (size_t)c->g.nx, (size_t)c->p.lf, (size_t)c->p.nf, cudaMemcpyDeviceToHost, c->stream));
@@ -832,6 +917,8 @@ int gpmood_adj_record(gpmood_ctx* c, int nsteps, int every, gpmood_adjoint** out
     if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
     if (c->p.bc_type == GPMOOD_DMR)
         return fail(c, GPMOOD_E_ARG, "adjoint: BC_type DMR (time-dependent inflow) is not supported");
+    if (c->p.integrator != GPMOOD_SSP_RK3 || c->p.num_flux != GPMOOD_HLLC)
+        return fail(c, GPMOOD_E_ARG, "adjoint: only SSP_RK3 with HLLC");
     gpmood_adjoint* a = new (std::nothrow) gpmood_adjoint();
     if (!a) return fail(c, GPMOOD_E_ARG, "out of host memory");
     a->c = c;

@@ -124,13 +124,13 @@ int stage_noalloc(const KernelTable& kt, const GridGeom& g, const GpWeights& w, 
 extern "C" int gpmood_time_stepping_noalloc(const gpmood_params* p, double* d_uin, double* d_uout, double t,
                                             double dt, void* stream) {
     if (!p || !d_uin || !d_uout) return nerr(GPMOOD_E_ARG, "NULL argument");
-    if (p->integrator != GPMOOD_SSP_RK3 || p->num_flux != GPMOOD_HLLC ||
+    if (p->integrator != GPMOOD_SSP_RK3 || p->num_flux < GPMOOD_HLLC || p->num_flux > GPMOOD_UNSPLIT ||
         (p->method != GPMOOD_GP_MOOD && p->method != GPMOOD_GP_SE) || !(p->mord == 1 || p->mord == 3 || p->mord == 5) ||
         p->ngp < 1 || p->ngp > 5 || p->lf < 4 || p->nf < 4 ||
         (p->bc_type != GPMOOD_NEUMANN && p->bc_type != GPMOOD_PERIODIC && p->bc_type != GPMOOD_REFLECTIVE &&
          p->bc_type != GPMOOD_DMR) ||
         (p->fp_mode != GPMOOD_FP_EXACT && p->fp_mode != GPMOOD_FP_FAST) || p->max_mood_iters < 0)
-        return nerr(GPMOOD_E_ARG, "unsupported knobs (GP_MOOD/GP_SE, SSP-RK3, HLLC, Mord 1/3/5, ngp 1..5)");
+        return nerr(GPMOOD_E_ARG, "unsupported knobs (GP_MOOD/GP_SE, SSP-RK3, Mord 1/3/5, ngp 1..5)");
     if (!(dt > 0) || dt != dt || dt > 1e300) return nerr(GPMOOD_E_DT, "dt must be finite and > 0");
     const size_t ncell = (size_t)(p->lf + 2 * GPM_NGC) * (size_t)(p->nf + 2 * GPM_NGC);
     if (ncell > GPM_NOALLOC_MAX_CELLS) {
@@ -163,6 +163,7 @@ extern "C" int gpmood_time_stepping_noalloc(const gpmood_params* p, double* d_ui
     g.ngp = p->ngp;
     g.mord = p->mord;
     g.method = p->method;
+    g.num_flux = p->num_flux;
     g.dmp = p->dmp;
     g.u2 = p->u2;
     g.u2_tol = p->u2_tol;

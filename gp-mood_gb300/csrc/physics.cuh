@@ -243,14 +243,139 @@ __device__ __forceinline__ void hllc(const double* ul, const double* ur, double*
     for (int k = 0; k < 4; k++) F[k] = Fk[k] + S * (st[k] * dStar - u[k]);
 }
 
+// Left/right wave-speed bounds and physical fluxes, as HLL_Flux and LLF_Flux
+// gather them (mod_HLL.f90:29-69, mod_LLF.f90:29-95); vxr is the right
+// state's x velocity for the 1/(vx-vx) of an inadmissible pair.
+struct LR {
+    double vmcl, vpcl, vmcr, vpcr, Fl[4], Fr[4], vxr;
+    bool adm;
+};
+
+template <int DIR>
+__device__ __forceinline__ LR lr_gather(const double* ul, const double* ur) {
+    LR r;
+#if GPM_EXACT
+    const Prim L = c2p<DIR>(ul), R = c2p<DIR>(ur);
+#else
+    const double rr = gpm_fast_rcp(ul[0] * ur[0]);
+    const Prim L = c2p<DIR>(ul, ur[0] * rr), R = c2p<DIR>(ur, ul[0] * rr);
+#endif
+    r.vmcl = L.vn - L.c;
+    r.vpcl = L.vn + L.c;
+    r.vmcr = R.vn - R.c;
+    r.vpcr = R.vn + R.c;
+    phys_flux<DIR>(ul, L, r.Fl);
+    phys_flux<DIR>(ur, R, r.Fr);
+    r.vxr = R.vx;
+    r.adm = L.adm && R.adm;
+    return r;
+}
+
+// HLL_Flux, mod_HLL.f90:11-169.
+template <int DIR>
+__device__ __forceinline__ void hll(const double* ul, const double* ur, double* F) {
+    const LR s = lr_gather<DIR>(ul, ur);
+    const double SL = fmin(s.vmcl, s.vmcr), SR = fmax(s.vpcl, s.vpcr);
+    if (!s.adm) {
+        const double bad = 1. / (s.vxr - s.vxr);
+        F[0] = F[1] = F[2] = F[3] = bad;
+    } else if (SL > 0.) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) F[k] = s.Fl[k];
+    } else if (SR < 0.) {
+#pragma unroll
+        for (int k = 0; k < 4; k++) F[k] = s.Fr[k];
+    } else {
+#pragma unroll
+        for (int k = 0; k < 4; k++) F[k] = ((SR * s.Fl[k] - SL * s.Fr[k]) + (SR * SL) * (ur[k] - ul[k])) / (SR - SL);
+    }
+}
+
+// LLF_Flux, mod_LLF.f90:11-175.
+template <int DIR>
+__device__ __forceinline__ void llf(const double* ul, const double* ur, double* F) {
+    const LR s = lr_gather<DIR>(ul, ur);
+    if (!s.adm) {
+        const double bad = 1. / (s.vxr - s.vxr);
+        F[0] = F[1] = F[2] = F[3] = bad;
+        return;
+    }
+    const double m = fmax(fmax(fmax(fabs(s.vmcl), fabs(s.vmcr)), fabs(s.vpcl)), fabs(s.vpcr));
+#pragma unroll
+    for (int k = 0; k < 4; k++) F[k] = 0.5 * (s.Fr[k] + s.Fl[k]) - (0.5 * m) * (ur[k] - ul[k]);
+}
+
+// unsplit_flux, mod_unsplit.f90:11-71.  An inadmissible pair gives
+// 1/(no-no) where no holds the right state's vy^2, the last value c2p_local
+// wrote to it.
+template <int DIR>
+__device__ __forceinline__ void unsplit(const double* ul, const double* ur, double* F) {
+#if GPM_EXACT
+    const Prim L = c2p<0>(ul), R = c2p<0>(ur);
+#else
+    const double rr = gpm_fast_rcp(ul[0] * ur[0]);
+    const Prim L = c2p<0>(ul, ur[0] * rr), R = c2p<0>(ur, ul[0] * rr);
+#endif
+    // c2p<0>: vn = vx, vt = vy
+    if (!(L.adm && R.adm)) {
+        const double no = R.vt * R.vt;
+        const double bad = 1. / (no - no);
+        F[0] = F[1] = F[2] = F[3] = bad;
+        return;
+    }
+    const double a = 1.1 * fmax(ul[0] * L.c, ur[0] * R.c);
+    const double vnL = DIR == 0 ? L.vn : L.vt, vnR = DIR == 0 ? R.vn : R.vt;
+    const double vtL = DIR == 0 ? L.vt : L.vn, vtR = DIR == 0 ? R.vt : R.vn;
+    const double pistar = 0.5 * (L.p + R.p) - (0.5 * a) * (vnR - vnL);
+    const double ustar = 0.5 * (vnL + vnR) - (0.5 * (R.p - L.p)) / a;
+    const double trans = -(0.5 * a) * (vtR - vtL);
+    const double* u = ustar > 0 ? ul : ur;
+#pragma unroll
+    for (int k = 0; k < 4; k++) F[k] = u[k] * ustar;
+    F[DIR == 0 ? 1 : 2] = F[DIR == 0 ? 1 : 2] + pistar;
+    F[DIR == 0 ? 2 : 1] = F[DIR == 0 ? 2 : 1] + trans;
+    F[3] = F[3] + pistar * ustar;
+}
+
+// The Riemann solvers other than HLLC as one out-of-line function per
+// direction, so that the many face-kernel instantiations inline only HLLC;
+// states pass by value (no local-memory arrays on the HLLC path).
+struct Flux4 {
+    double f[4];
+};
+
+template <int DIR>
+__device__ __noinline__ Flux4 riemann_other(int nflux, double l0, double l1, double l2, double l3, double r0,
+                                            double r1, double r2, double r3) {
+    const double ul[4] = {l0, l1, l2, l3}, ur[4] = {r0, r1, r2, r3};
+    Flux4 F;
+    if (nflux == 101) llf<DIR>(ul, ur, F.f);
+    else if (nflux == 102) hll<DIR>(ul, ur, F.f);
+    else unsplit<DIR>(ul, ur, F.f);
+    return F;
+}
+
+// The Riemann solver of numFlux (mod_FE.f90:84-91); nflux is the same for
+// every thread of a launch, so the switch does not diverge.
+template <int DIR>
+__device__ __forceinline__ void riemann(int nflux, const double* ul, const double* ur, double* F) {
+    if (nflux == 100) {
+        hllc<DIR>(ul, ur, F);
+    } else {
+        const Flux4 r = riemann_other<DIR>(nflux, ul[0], ul[1], ul[2], ul[3], ur[0], ur[1], ur[2], ur[3]);
+        F[0] = r.f[0]; F[1] = r.f[1]; F[2] = r.f[2]; F[3] = r.f[3];
+    }
+}
+
 // Face flux with Gauss quadrature, mod_FE.f90:80-98: sum_g Fg*w_g from zero.
 template <int DIR, int NGP>
-__device__ __forceinline__ void quad_flux(const double (*uL)[4], const double (*uR)[4], const double* gw, double* F) {
+__device__ __forceinline__ void quad_flux(const double (*uL)[4], const double (*uR)[4], const double* gw, double* F,
+                                          int nflux = 100) {
     double acc[4];
 #pragma unroll
     for (int g = 0; g < NGP; g++) {
         double Fg[4];
-        hllc<DIR>(uL[g], uR[g], Fg);
+        riemann<DIR>(nflux, uL[g], uR[g], Fg);
 #pragma unroll
         for (int k = 0; k < 4; k++) acc[k] = (g == 0) ? Fg[k] * gw[0] : acc[k] + Fg[k] * gw[g];
     }

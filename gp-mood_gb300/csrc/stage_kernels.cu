@@ -152,7 +152,7 @@ __device__ __forceinline__ void recon_face(const GpWeights& w, int o, int face, 
 
 template <int DIR, int NP, int NGP>
 __device__ __forceinline__ void face_from_tile(const GpWeights& w, int o, const Cell (*tile)[HX], int tx, int ty,
-                                               double* F) {
+                                               double* F, int nflux) {
     constexpr int FL = DIR == 0 ? 2 : 1;  // iR (x) / iT (y) face of the low cell
     constexpr int FH = DIR == 0 ? 0 : 3;  // iL (x) / iB (y) face of the high cell
     double uL[NGP][4], uR[NGP][4];
@@ -169,7 +169,7 @@ __device__ __forceinline__ void face_from_tile(const GpWeights& w, int o, const 
         for (int m = 0; m < NP; m++) q[m] = tile[ty + hy + st_oy(m)][tx + hx + st_ox(m)];
         recon_face<DIR, NP, NGP>(w, o, FH, q, uR);
     }
-    quad_flux<DIR, NGP>(uL, uR, w.gw, F);
+    quad_flux<DIR, NGP>(uL, uR, w.gw, F, nflux);
 }
 
 template <int DIR, int NGP, int UORD>  // UORD: uniform order (1,3,5) or 0 = per-face from the order array
@@ -190,13 +190,13 @@ __global__ void __launch_bounds__(TX * TY) k_flux_tile(StageArgs a, const __grid
     const int tx = threadIdx.x + 2, ty = threadIdx.y + 2;
     double F[4];
     if (UORD != 0) {
-        face_from_tile<DIR, np_of(UORD == 0 ? 1 : UORD), NGP>(w, UORD / 2, tile, tx, ty, F);
+        face_from_tile<DIR, np_of(UORD == 0 ? 1 : UORD), NGP>(w, UORD / 2, tile, tx, ty, F, g.num_flux);
     } else {
         const size_t c0 = cidx(g, l, n), c1 = DIR == 0 ? c0 + 1 : c0 + g.nx;
         const int o = min((int)a.order[c0], (int)a.order[c1]);
-        if (o >= 5) face_from_tile<DIR, 13, NGP>(w, 2, tile, tx, ty, F);
-        else if (o >= 3) face_from_tile<DIR, 5, NGP>(w, 1, tile, tx, ty, F);
-        else face_from_tile<DIR, 1, NGP>(w, 0, tile, tx, ty, F);
+        if (o >= 5) face_from_tile<DIR, 13, NGP>(w, 2, tile, tx, ty, F, g.num_flux);
+        else if (o >= 3) face_from_tile<DIR, 5, NGP>(w, 1, tile, tx, ty, F, g.num_flux);
+        else face_from_tile<DIR, 1, NGP>(w, 0, tile, tx, ty, F, g.num_flux);
     }
     double* out = (DIR == 0 ? a.fx : a.fy) + 4 * cidx(g, l, n);
     st_cell(out, Cell{F[0], F[1], F[2], F[3]});
@@ -396,7 +396,7 @@ __device__ __forceinline__ void edge_faces(const GridGeom& g, const GpWeights& w
 }
 
 // One cell tile per block (x fastest).
-__global__ void __launch_bounds__(XT * XY, 2) k_flux_xy(StageArgs a, const __grid_constant__ GpWeights w, int tiles_x) {
+__global__ void __launch_bounds__(XT * XY) k_flux_xy(StageArgs a, const __grid_constant__ GpWeights w, int tiles_x) {
     extern __shared__ __align__(16) unsigned char xy_raw[];
     XySmem& sm = *reinterpret_cast<XySmem*>(xy_raw);
     const int by = blockIdx.x / tiles_x, bx = blockIdx.x - by * tiles_x;
@@ -441,7 +441,8 @@ void launch_flux_ngp(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
 
 int launch_flux_all(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
 #if !GPM_EXACT
-    if (a.uniform_order && a.g.mord == 5 && a.g.ngp == 3 && launch_flux_xy(a, w, s)) return 2;
+    if (a.uniform_order && a.g.mord == 5 && a.g.ngp == 3 && a.g.num_flux == 100 && launch_flux_xy(a, w, s))
+        return 2;
 #endif
     switch (a.g.ngp) {
     case 1: launch_flux_ngp<1>(a, w, s); break;
@@ -575,7 +576,7 @@ __device__ __forceinline__ void face_global(const GridGeom& g, const GpWeights& 
         for (int m = 0; m < NP; m++) q[m] = ld_cell(uin + 4 * (c1 + st_ox(m) + row * st_oy(m)));
         recon_face<DIR, NP, NGP>(w, o, FH, q, uR);
     }
-    quad_flux<DIR, NGP>(uL, uR, w.gw, F);
+    quad_flux<DIR, NGP>(uL, uR, w.gw, F, g.num_flux);
 }
 
 template <int DIR, int NGP>
@@ -857,6 +858,45 @@ __global__ void __launch_bounds__(256) k_combine(GridGeom g, const double* __res
     if (with_cfl) dt_reduce(v, sc);
 }
 
+// y = c[0]*x[0] + c[1]*x[1] + ... (n terms, summed left to right as the
+// reference's whole-array expressions of mod_SSP_RK4.f90:25-36 and
+// mod_FE.f90:188), over every cell; y may be one of the x.
+struct LinComb {
+    const double* x[5];
+    double c[5];
+    int n;
+};
+
+__global__ void __launch_bounds__(256) k_lincomb(GridGeom g, double* y, LinComb lc, int with_cfl, DevScalars* sc) {
+    const size_t ncell = (size_t)g.nx * g.ny;
+    double v = 1.0e30;
+    for (size_t c = blockIdx.x * (size_t)blockDim.x + threadIdx.x; c < ncell; c += (size_t)gridDim.x * blockDim.x) {
+        const Cell a = ld_cell_cg(lc.x[0] + 4 * c);
+        Cell o{lc.c[0] * a.r, lc.c[0] * a.mx, lc.c[0] * a.my, lc.c[0] * a.e};
+        for (int i = 1; i < lc.n; i++) {
+            const Cell b = ld_cell_cg(lc.x[i] + 4 * c);
+            o.r = o.r + lc.c[i] * b.r;
+            o.mx = o.mx + lc.c[i] * b.mx;
+            o.my = o.my + lc.c[i] * b.my;
+            o.e = o.e + lc.c[i] * b.e;
+        }
+        st_cell(y + 4 * c, o);
+        if (with_cfl) v = fmin(v, cell_dt(o, g.dx, g.dy));
+    }
+    if (with_cfl) dt_reduce(v, sc);
+}
+
+void launch_lincomb(const GridGeom& g, double* y, int n, const double* const* x, const double* c, int with_cfl,
+                    DevScalars* sc, cudaStream_t s) {
+    LinComb lc{};
+    lc.n = n;
+    for (int i = 0; i < n; i++) {
+        lc.x[i] = x[i];
+        lc.c[i] = c[i];
+    }
+    k_lincomb<<<list_grid(g.nx * g.ny, 256), 256, 0, s>>>(g, y, lc, with_cfl, sc);
+}
+
 void launch_combine(const GridGeom& g, const double* x, double* y, double a, double b, int with_cfl, DevScalars* sc,
                     cudaStream_t s) {
     k_combine<<<list_grid(g.nx * g.ny, 256), 256, 0, s>>>(g, x, y, a, b, with_cfl, sc);
@@ -886,7 +926,7 @@ void launch_advance_t(DevScalars* sc, cudaStream_t s) { k_advance_t<<<1, 1, 0, s
 
 const KernelTable table = {launch_bc,          launch_flux_all,   launch_update_detect, launch_mood_mark,
                            launch_mood_faces,  launch_mood_cells, launch_combine,       launch_cfl,
-                           launch_dt_finalize, launch_advance_t,  launch_mood_loop};
+                           launch_dt_finalize, launch_advance_t,  launch_mood_loop,     launch_lincomb};
 
 }  // namespace GPM_NS
 
@@ -904,7 +944,7 @@ __device__ __forceinline__ GridGeom bgeom(const BatchArgs& a, const BProb& p) {
     g.lf = p.lf; g.nf = p.nf; g.nx = p.nx; g.ny = p.ny;
     g.dx = p.dx; g.dy = p.dy;
     g.bc_type = a.bc_type; g.ngp = a.ngp; g.mord = a.mord; g.method = a.method;
-    g.dmp = a.dmp; g.u2 = a.u2; g.u2_tol = a.u2_tol; g.pad = 0;
+    g.dmp = a.dmp; g.u2 = a.u2; g.u2_tol = a.u2_tol; g.num_flux = a.num_flux;
     return g;
 }
 
@@ -964,7 +1004,8 @@ void blaunch_bc(const BatchArgs& a, double* u, cudaStream_t s) {
 // Face tiles of every problem: a persistent CTA walks the tile list.  Tile
 // shape TXB x TYB is a template parameter chosen by the autotuner.
 template <int DIR, int NP, int NGP, int HXB>
-__device__ __forceinline__ void face_tile_b(const GpWeights& w, int o, const Cell* tile, int tx, int ty, double* F) {
+__device__ __forceinline__ void face_tile_b(const GpWeights& w, int o, const Cell* tile, int tx, int ty, double* F,
+                                            int nflux) {
     constexpr int FL = DIR == 0 ? 2 : 1;
     constexpr int FH = DIR == 0 ? 0 : 3;
     double uL[NGP][4], uR[NGP][4];
@@ -981,7 +1022,7 @@ __device__ __forceinline__ void face_tile_b(const GpWeights& w, int o, const Cel
         for (int m = 0; m < NP; m++) q[m] = tile[(ty + hy + st_oy(m)) * HXB + tx + hx + st_ox(m)];
         recon_face<DIR, NP, NGP>(w, o, FH, q, uR);
     }
-    quad_flux<DIR, NGP>(uL, uR, w.gw, F);
+    quad_flux<DIR, NGP>(uL, uR, w.gw, F, nflux);
 }
 
 template <int TXB, int TYB, int NGP, int ORD>
@@ -1005,8 +1046,9 @@ __global__ void __launch_bounds__(TXB* TYB) kb_flux(BatchArgs a) {
         const int l = it.z + threadIdx.x, n = it.w + threadIdx.y;
         if (l > g.lf || n > g.nf) continue;
         double F[4];
-        if (it.y == 0) face_tile_b<0, np_of(ORD), NGP, HXB>(w, ORD / 2, tile, threadIdx.x + 2, threadIdx.y + 2, F);
-        else face_tile_b<1, np_of(ORD), NGP, HXB>(w, ORD / 2, tile, threadIdx.x + 2, threadIdx.y + 2, F);
+        if (it.y == 0)
+            face_tile_b<0, np_of(ORD), NGP, HXB>(w, ORD / 2, tile, threadIdx.x + 2, threadIdx.y + 2, F, g.num_flux);
+        else face_tile_b<1, np_of(ORD), NGP, HXB>(w, ORD / 2, tile, threadIdx.x + 2, threadIdx.y + 2, F, g.num_flux);
         st_cell((it.y == 0 ? a.fx : a.fy) + 4 * (P.off + (long long)cidx(g, l, n)), Cell{F[0], F[1], F[2], F[3]});
     }
 }

@@ -23,8 +23,8 @@ LIB_PATH = HERE / "libgpmood.so"
 NGC = 4
 # gp-mood-code/constants.f90:17-34
 GP_MOOD, GP_SE, NN_GP_MOOD = 2, 202, 203
-SSP_RK3 = 10
-HLLC = 100
+FE, SSP_RK2, SSP_RK3, SSP_RK4 = 8, 9, 10, 12
+HLLC, LLF, HLL, UNSPLIT = 100, 101, 102, 103
 NEUMANN, PERIODIC, REFLECTIVE, DMR = 17, 18, 20, 35
 FP_EXACT, FP_FAST = 0, 1
 

@@ -39,8 +39,14 @@ extern "C" {
 #define GPMOOD_GP_MOOD     2     /* method: GP-MOOD */
 #define GPMOOD_GP_SE       202   /* method: unlimited GP (MOOD off) */
 #define GPMOOD_NN_GP_MOOD  203   /* method: GP-MOOD with the MLP a-priori gate */
-#define GPMOOD_SSP_RK3     10    /* integrator */
+#define GPMOOD_FE          8     /* integrator: Forward_Euler */
+#define GPMOOD_SSP_RK2     9
+#define GPMOOD_SSP_RK3     10
+#define GPMOOD_SSP_RK4     12
 #define GPMOOD_HLLC        100   /* numFlux */
+#define GPMOOD_LLF         101
+#define GPMOOD_HLL         102
+#define GPMOOD_UNSPLIT     103
 #define GPMOOD_NEUMANN     17    /* BC_type */
 #define GPMOOD_PERIODIC    18
 #define GPMOOD_REFLECTIVE  20
@@ -65,12 +71,12 @@ typedef struct gpmood_params {
     double ell_o_dx;      /* GP length scale in cells                  :14 */
     double lx, ly;        /* domain [0,Lx]x[0,Ly] (Lx_16, Ly_16)       :43-44 */
     double tmax;          /* final time                                :41 */
-    int integrator;       /* must be GPMOOD_SSP_RK3                    :9  */
+    int integrator;       /* GPMOOD_FE, _SSP_RK2, _SSP_RK3, _SSP_RK4   :9  */
     int method;           /* GPMOOD_GP_MOOD, GPMOOD_GP_SE, GPMOOD_NN_GP_MOOD */
     int mord;             /* maximal order 1, 3 or 5                   :15 */
     int ngp;              /* Gauss points per face, 1..5               :16 */
     int dmp, u2, u2_tol;  /* MOOD checks (logical -> 0/1)              :18-20 */
-    int num_flux;         /* must be GPMOOD_HLLC                       :30 */
+    int num_flux;         /* GPMOOD_HLLC, _LLF, _HLL, _UNSPLIT         :30 */
     int lf, nf;           /* interior cells in x and y                 :37-38 */
     int bc_type;          /* GPMOOD_NEUMANN/PERIODIC/REFLECTIVE/DMR    :45 */
     int nmax;             /* step cap of the time loop                 :42 */

@@ -367,6 +367,92 @@ void orc_hllc(const double* ul, const double* ur, int dir, double* F)
     }
 }
 
+/* The left and right states' primitive data in the face-normal frame, as
+ * HLL_Flux / LLF_Flux gather them (mod_HLL.f90:29-69, mod_LLF.f90:29-95). */
+typedef struct { double vmcl, vpcl, vmcr, vpcr, Fl[4], Fr[4], vx_last; int adm; } lr_state;
+
+static lr_state lr_gather(const double* ul, const double* ur, int dir)
+{
+    lr_state s;
+    double vx, vy, vx2, vy2, pres, c;
+    s.adm = 1;
+    c2p_local(ul, &vx, &vy, &vx2, &vy2, &pres, &c, &s.adm);
+    s.vmcl = (dir == 1 ? vx : vy) - c;
+    s.vpcl = (dir == 1 ? vx : vy) + c;
+    phys_flux(ul, dir, vx, vy, vx2, vy2, pres, s.Fl);
+    c2p_local(ur, &vx, &vy, &vx2, &vy2, &pres, &c, &s.adm);
+    s.vmcr = (dir == 1 ? vx : vy) - c;
+    s.vpcr = (dir == 1 ? vx : vy) + c;
+    phys_flux(ur, dir, vx, vy, vx2, vy2, pres, s.Fr);
+    s.vx_last = vx;
+    return s;
+}
+
+/* HLL_Flux, mod_HLL.f90:11-169 */
+void orc_hll(const double* ul, const double* ur, int dir, double* F)
+{
+    lr_state s = lr_gather(ul, ur, dir);
+    const double SL = fmin(s.vmcl, s.vmcr), SR = fmax(s.vpcl, s.vpcr);
+    if (!s.adm) {
+        for (int k = 0; k < 4; k++) F[k] = 1. / (s.vx_last - s.vx_last);
+        return;
+    }
+    if (SL > 0.) {
+        for (int k = 0; k < 4; k++) F[k] = s.Fl[k];
+    } else if (SR < 0.) {
+        for (int k = 0; k < 4; k++) F[k] = s.Fr[k];
+    } else {
+        for (int k = 0; k < 4; k++) F[k] = ((SR * s.Fl[k] - SL * s.Fr[k]) + (SR * SL) * (ur[k] - ul[k])) / (SR - SL);
+    }
+}
+
+/* LLF_Flux, mod_LLF.f90:11-175 */
+void orc_llf(const double* ul, const double* ur, int dir, double* F)
+{
+    lr_state s = lr_gather(ul, ur, dir);
+    if (!s.adm) {
+        for (int k = 0; k < 4; k++) F[k] = 1. / (s.vx_last - s.vx_last);
+        return;
+    }
+    /* max(abs(vmcl), abs(vmcr), abs(vpcl), abs(vpcr)) */
+    const double m = fmax(fmax(fmax(fabs(s.vmcl), fabs(s.vmcr)), fabs(s.vpcl)), fabs(s.vpcr));
+    for (int k = 0; k < 4; k++) F[k] = 0.5 * (s.Fr[k] + s.Fl[k]) - (0.5 * m) * (ur[k] - ul[k]);
+}
+
+/* unsplit_flux, mod_unsplit.f90:11-71 */
+void orc_unsplit(const double* ul, const double* ur, int dir, double* F)
+{
+    double vxL, vyL, vxR, vyR, pL, pR, cL, cR, no;
+    int adm = 1;
+    c2p_local(ul, &vxL, &vyL, &no, &no, &pL, &cL, &adm);
+    c2p_local(ur, &vxR, &vyR, &no, &no, &pR, &cR, &adm); /* no = vy_R^2, written last */
+    const double a = 1.1 * fmax(ul[RHO] * cL, ur[RHO] * cR);
+    double pistar, ustar, trans;
+    if (dir == 1) {
+        pistar = 0.5 * (pL + pR) - (0.5 * a) * (vxR - vxL);
+        ustar = 0.5 * (vxL + vxR) - (0.5 * (pR - pL)) / a;
+        trans = -(0.5 * a) * (vyR - vyL);
+    } else {
+        pistar = 0.5 * (pL + pR) - (0.5 * a) * (vyR - vyL);
+        ustar = 0.5 * (vyL + vyR) - (0.5 * (pR - pL)) / a;
+        trans = -(0.5 * a) * (vxR - vxL);
+    }
+    if (!adm) {
+        for (int k = 0; k < 4; k++) F[k] = 1. / (no - no);
+        return;
+    }
+    const double* u = ustar > 0 ? ul : ur;
+    for (int k = 0; k < 4; k++) F[k] = u[k] * ustar;
+    if (dir == 1) {
+        F[MOMX] = F[MOMX] + pistar;
+        F[MOMY] = F[MOMY] + trans;
+    } else {
+        F[MOMY] = F[MOMY] + pistar;
+        F[MOMX] = F[MOMX] + trans;
+    }
+    F[ENER] = F[ENER] + pistar * ustar;
+}
+
 /* ------------------------------------------------------------------ */
 /* Grid helpers */
 
@@ -511,6 +597,7 @@ struct orc_ctx {
     int *cellgpo;  /* CellGPO, :59 */
     unsigned char *detcell, *detfx, *detfy, *decrease;
     double *u1, *u2;
+    double *rk4[5];  /* U3, U4, FU3, FU4, Fl of SSP_RK4_ (U1, U2 are u1, u2), on first use */
 };
 
 orc_ctx* orc_create(const orc_params* p)
@@ -546,6 +633,7 @@ void orc_destroy(orc_ctx* c)
     if (!c) return;
     free(c->uh); free(c->lfx); free(c->lfy); free(c->cellgpo); free(c->detcell);
     free(c->detfx); free(c->detfy); free(c->decrease); free(c->u1); free(c->u2);
+    for (int i = 0; i < 5; i++) free(c->rk4[i]);
     free(c);
 }
 
@@ -603,7 +691,12 @@ static void face_flux(const orc_ctx* c, size_t cl, size_t cr, int dir, double* o
     for (int j = 0; j < ngp; j++) {
         const double* uL = UH(c, cl, dir == 1 ? IR : IT, j);
         const double* uR = UH(c, cr, dir == 1 ? IL : IB, j);
-        orc_hllc(uL, uR, dir, Fg[j]);
+        switch (c->p.num_flux) { /* mod_FE.f90:84-91 */
+        case 101: orc_llf(uL, uR, dir, Fg[j]); break;
+        case 102: orc_hll(uL, uR, dir, Fg[j]); break;
+        case 103: orc_unsplit(uL, uR, dir, Fg[j]); break;
+        default: orc_hllc(uL, uR, dir, Fg[j]); break;
+        }
     }
     for (int k = 0; k < 4; k++) {
         double s = 0.0;
@@ -810,6 +903,8 @@ int orc_forward_euler(orc_ctx* c, double* Uin, double* Uout, double dt, double t
         for (int n = 1; n <= G.nf; n++)
             for (int l = 1; l <= G.lf; l++)
                 final_order[(size_t)(n - 1) * G.lf + (l - 1)] = (signed char)c->cellgpo[CIDX(G, l, n)];
+    if (p->integrator == 12) /* SSP_RK4 takes the increment dt*L(Uin), mod_FE.f90:188 */
+        for (size_t i = 0; i < nc * 4; i++) Uout[i] = Uout[i] - Uin[i];
     return 0;
 }
 
@@ -819,6 +914,48 @@ int orc_time_stepping(orc_ctx* c, double* Uin, double* Uout, double t, double dt
 {
     const size_t n4 = c->ncell * 4;
     int rc;
+#define ORC_FE(k, in, out, trk) \
+    orc_forward_euler(c, in, out, dt, trk, (init_orders && (k) < 3) ? init_orders[k] : NULL, \
+                      (stage_orders && (k) < 3) ? stage_orders[k] : NULL, counters)
+    const int integ = c->p.integrator ? c->p.integrator : 10;
+    /* time_stepper.f90:17-21: t_rk = t unless SSP_RK3_ moves it */
+    if (integ == 8) return ORC_FE(0, Uin, Uout, t);
+    if (integ == 9) { /* SSP_RK2_, mod_SSP_RK2.f90:12-24 */
+        if ((rc = ORC_FE(0, Uin, c->u1, t))) return rc;
+        if ((rc = ORC_FE(1, c->u1, Uout, t))) return rc;
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < n4; i++) Uout[i] = 0.5 * (Uin[i] + Uout[i]);
+        return 0;
+    }
+    if (integ == 12) { /* SSP_RK4_, mod_SSP_RK4.f90:12-38 with the constants of constants.f90:46-51 */
+        const double c1 = 0.391752226571890, a20 = 0.444370493651235, a21 = 0.555629506348765,
+                     c2 = 0.368410593050371, a30 = 0.620101851488403, a32 = 0.379898148511597,
+                     c3 = 0.251891774271694, a40 = 0.178079954393132, a43 = 0.821920045606868,
+                     c4 = 0.544974750228521, f2 = 0.517231671970585, f3 = 0.096059710526147,
+                     f4 = 0.386708617503269, ff3 = 0.063692468666290, ff4 = 0.226007483236906;
+        for (int i = 0; i < 5; i++)
+            if (!c->rk4[i] && !(c->rk4[i] = (double*)malloc(c->ncell * 32))) return -3;
+        double *U1 = c->u1, *U2 = c->u2, *U3 = c->rk4[0], *U4 = c->rk4[1], *FU3 = c->rk4[2], *FU4 = c->rk4[3],
+               *Fl = c->rk4[4];
+        if ((rc = ORC_FE(0, Uin, Fl, t))) return rc;
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < n4; i++) U1[i] = Uin[i] + c1 * Fl[i];
+        if ((rc = ORC_FE(1, U1, Fl, t))) return rc;
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < n4; i++) U2[i] = a20 * Uin[i] + a21 * U1[i] + c2 * Fl[i];
+        if ((rc = ORC_FE(2, U2, Fl, t))) return rc;
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < n4; i++) U3[i] = a30 * Uin[i] + a32 * U2[i] + c3 * Fl[i];
+        if ((rc = ORC_FE(3, U3, FU3, t))) return rc;
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < n4; i++) U4[i] = a40 * Uin[i] + a43 * U3[i] + c4 * FU3[i];
+        if ((rc = ORC_FE(4, U4, FU4, t))) return rc;
+#pragma omp parallel for schedule(static)
+        for (size_t i = 0; i < n4; i++)
+            Uout[i] = f2 * U2[i] + f3 * U3[i] + ff3 * FU3[i] + f4 * U4[i] + ff4 * FU4[i];
+        return 0;
+    }
+#undef ORC_FE
     /* SSP_RK3_, mod_SSP_RK3.f90:12-39 */
     rc = orc_forward_euler(c, Uin, c->u1, dt, t, init_orders ? init_orders[0] : NULL,
                            stage_orders ? stage_orders[0] : NULL, counters);

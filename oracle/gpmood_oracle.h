@@ -37,6 +37,8 @@ typedef struct orc_params {
     int dmp, u2, u2_tol;
     int lf, nf;        /* interior cells */
     int bc_type;       /* 17 Neumann, 18 Periodic, 20 Reflective, 35 DMR */
+    int integrator;    /* 8 FE, 9 SSP_RK2, 10 SSP_RK3 (default for 0), 12 SSP_RK4 (constants.f90:19) */
+    int num_flux;      /* 100 HLLC (default for 0), 101 LLF, 102 HLL, 103 unsplit (constants.f90:21) */
 } orc_params;
 
 /* GP weights as produced by GP_presim_sphere (GP_init.f90:26-357).
@@ -55,6 +57,9 @@ int  orc_gp_presim(const orc_params* p, orc_gp* out);
 
 /* Physics kernels (physics.f90, mod_HLLC.f90). */
 void orc_hllc(const double ul[4], const double ur[4], int dir, double F[4]);
+void orc_hll(const double ul[4], const double ur[4], int dir, double F[4]);
+void orc_llf(const double ul[4], const double ur[4], int dir, double F[4]);
+void orc_unsplit(const double ul[4], const double ur[4], int dir, double F[4]);
 double orc_pressure(const double u[4]);
 
 /* Boundary_C (BC.f90:10-135, 283-341) on a full padded array. */

@@ -23,13 +23,15 @@ NGC = 4
 # constants.f90:17-34
 GP_MOOD, GP_SE = 2, 202
 NEUMANN, PERIODIC, REFLECTIVE, DMR = 17, 18, 20, 35
+FE, SSP_RK2, SSP_RK3, SSP_RK4 = 8, 9, 10, 12
+HLLC, LLF, HLL, UNSPLIT = 100, 101, 102, 103
 
 
 class OrcParams(C.Structure):
     _fields_ = [("cfl", C.c_double), ("ell_o_dx", C.c_double), ("lx", C.c_double), ("ly", C.c_double),
                 ("tmax", C.c_double), ("mord", C.c_int), ("ngp", C.c_int), ("method", C.c_int),
                 ("dmp", C.c_int), ("u2", C.c_int), ("u2_tol", C.c_int), ("lf", C.c_int), ("nf", C.c_int),
-                ("bc_type", C.c_int)]
+                ("bc_type", C.c_int), ("integrator", C.c_int), ("num_flux", C.c_int)]
 
 
 class OrcGp(C.Structure):
@@ -87,8 +89,9 @@ def lib() -> C.CDLL:
 
 
 def make_params(lf, nf, *, lx=1.0, ly=1.0, tmax=0.8, mord=5, ngp=3, method=GP_MOOD, bc=NEUMANN, cfl=0.8,
-                ell_o_dx=12.0, dmp=1, u2=1, u2_tol=1) -> OrcParams:
-    return OrcParams(cfl, ell_o_dx, lx, ly, tmax, mord, ngp, method, dmp, u2, u2_tol, lf, nf, bc)
+                ell_o_dx=12.0, dmp=1, u2=1, u2_tol=1, integrator=SSP_RK3, num_flux=HLLC) -> OrcParams:
+    return OrcParams(cfl, ell_o_dx, lx, ly, tmax, mord, ngp, method, dmp, u2, u2_tol, lf, nf, bc, integrator,
+                     num_flux)
 
 
 def padded(lf: int, nf: int) -> np.ndarray:

@@ -41,7 +41,7 @@ def test_default_params_are_the_reference_knobs(pkg):
     assert (p.dmp, p.u2, p.u2_tol, p.method) == (1, 1, 1, 2)
 
 
-@pytest.mark.parametrize("bad", [dict(mord=7), dict(ngp=6), dict(num_flux=103), dict(integrator=12),
+@pytest.mark.parametrize("bad", [dict(mord=7), dict(ngp=6), dict(num_flux=104), dict(integrator=11),
                                  dict(bc_type=19), dict(lf=2), dict(method=200), dict(fp_mode=3),
                                  dict(max_mood_iters=-1), dict(cfl=0.0)])
 def test_invalid_knobs_rejected(pkg, bad):

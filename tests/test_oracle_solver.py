@@ -105,3 +105,18 @@ def test_deprecated_inversion_error_anchor(oracle, n, ref):
     assert ref / 4 <= err <= ref * 4, (err, ref)
     if n == 100:
         assert err == ref  # identical to the last bit
+
+
+@pytest.mark.parametrize("integ,nflux", [(10, 101), (10, 102), (10, 103), (8, 100), (9, 100), (12, 100)])
+def test_variants_conserve_mass_and_symmetry(oracle, integ, nflux):
+    """Periodic isentropic vortex: every Riemann solver / integrator conserves
+    the totals to rounding; the x<->y symmetric 2DRP3 stays symmetric."""
+    p = oracle.make_params(32, 32, bc=18, lx=10.0, ly=10.0, tmax=1.0, integrator=integ, num_flux=nflux)
+    U, t, k, _ = run(oracle, p, "vortex", 4)
+    U0 = oracle.initial_condition(p, "vortex")
+    for v in range(4):
+        assert abs(U[I + (v,)].sum() - U0[I + (v,)].sum()) <= 1e-12 * abs(U0[I + (v,)]).sum()
+    p = oracle.make_params(32, 32, bc=17, tmax=0.8, integrator=integ, num_flux=nflux)
+    U, t, k, _ = run(oracle, p, "rp2d3", 4)
+    r = U[I + (0,)]
+    assert np.abs(r - r.T).sum() / r.size < 1e-12  # plot/plotter_hdf5.py:43, as above
