@@ -57,7 +57,9 @@ def parse():
     ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batched form (0: skip)")
     ap.add_argument("--adjoint", type=int, default=1, help="also time the adjoint form (0: skip)")
     ap.add_argument("--final", action="store_true",
-                    help="run plain and NN-gated GP-MOOD from t=0 to t_final=0.05 and compare them")
+                    help="run plain (and NN-gated unless --nn 0) GP-MOOD from t=0 to t_final and compare them")
+    ap.add_argument("--case", choices=("sedov", "rp2d3", "dmr"), default="sedov",
+                    help="problem of --final: Sedov n^2 (t_final 0.05), 2DRP3 256^2 (0.8), DMR 4096x1024 (0.2)")
     return ap.parse_args()
 
 
@@ -314,24 +316,37 @@ def measure_adjoint(pkg):
                       "backward includes the segment recomputation)"}
 
 
+# Whole runs of the benchmark problems (t = 0 to t_final): name -> (IC builder
+# name, lf, nf, Lx, Ly, BC, t_final).
+FINAL_CASES = {
+    "sedov": ("sedov", None, None, 1.0, 1.0, 20, TMAX),
+    "rp2d3": ("rp2d3", 256, 256, 1.0, 1.0, 17, 0.8),
+    "dmr": ("dmr", 4096, 1024, 4.0, 1.0, 35, 0.2),
+}
+
+
 def run_final(args):
-    """Plain and NN-gated GP-MOOD on the Sedov problem from t=0 to t_final:
-    time to solution, steps, and the relative L1 difference of the final states."""
+    """Plain (and, unless --nn 0, NN-gated) GP-MOOD from t = 0 to t_final on one
+    of the benchmark problems: time to solution, steps, and the relative L1
+    difference of the final states."""
     import numpy as np
     import torch
     import __graft_entry__ as ge
     pkg = ge.import_package()
     from gpmood_gb300 import ic, nn_train as T
-    n = args.n
+    icname, lf, nf, lx, ly, bc, tfinal = FINAL_CASES[args.case]
+    lf = lf or args.n
+    nf = nf or args.n
     fp = pkg.FP_FAST if args.fp_mode == "fast" else pkg.FP_EXACT
-    U0 = ic.sedov(n, n)
+    U0 = getattr(ic, icname)(lf, nf) if icname != "dmr" else ic.dmr(lf, nf, lx, ly)
     params = T.load_text(str(GATE))
     meta_f = GATE.with_suffix(".json")
     thr = float(json.loads(meta_f.read_text()).get("threshold", 0.0)) if meta_f.exists() else 0.0
     out = {}
     finals = {}
-    for name, method in (("plain", pkg.GP_MOOD), ("nn_gated", pkg.NN_GP_MOOD)):
-        with pkg.Solver(lf=n, nf=n, bc_type=pkg.REFLECTIVE, tmax=TMAX, fp_mode=fp, method=method) as s:
+    variants = [("plain", pkg.GP_MOOD)] + ([("nn_gated", pkg.NN_GP_MOOD)] if args.nn else [])
+    for name, method in variants:
+        with pkg.Solver(lf=lf, nf=nf, lx=lx, ly=ly, bc_type=bc, tmax=tfinal, fp_mode=fp, method=method) as s:
             s.Boundary_C(U0, 0.0)
             if method == pkg.NN_GP_MOOD:
                 s.set_nn(params)
@@ -350,13 +365,17 @@ def run_final(args):
             c = s.counters()
             tm = s.timing()
         finals[name] = U
-        out[name] = {"steps": steps, "t": t, "seconds": ms / 1e3, "value": n * n * steps / (ms * 1e-3),
+        out[name] = {"steps": steps, "t": t, "seconds": ms / 1e3, "value": lf * nf * steps / (ms * 1e-3),
                      "unit": "cell-updates/s", "detected_total": c.detected_total,
                      "max_passes_stage": c.max_passes_stage, "status_flags": c.status_flags,
-                     "mood_share": tm.mood_ms / ms if ms else None}
-    out["nn_gated"]["speedup_vs_plain"] = out["plain"]["seconds"] / out["nn_gated"]["seconds"]
-    out["rel_l1_final"] = _rel_l1(finals["nn_gated"], finals["plain"])
-    line = {"metric": "time to t_final", "workload": workload_name(n) + f", t_final={TMAX}",
+                     "flux_share": tm.flux_ms / ms if ms else None, "mood_share": tm.mood_ms / ms if ms else None,
+                     "final_state": {"sum_rho": float(U[4:-4, 4:-4, 0].sum()), "sum_E": float(U[4:-4, 4:-4, 3].sum())}}
+    if args.nn:
+        out["nn_gated"]["speedup_vs_plain"] = out["plain"]["seconds"] / out["nn_gated"]["seconds"]
+        out["rel_l1_final"] = _rel_l1(finals["nn_gated"], finals["plain"])
+    line = {"metric": "time to t_final", "case": args.case,
+            "workload": f"{icname} {lf}x{nf} on [0,{lx:g}]x[0,{ly:g}], BC {bc}, t_final={tfinal}, plain GP-MOOD "
+                        f"Mord=5 (R2->R1->1), ngp=3, ell=12dx, HLLC, SSP-RK3, CFL 0.8",
             "fp_mode": args.fp_mode, "gate": GATE.name, "logit_threshold": thr, **out}
     print(json.dumps(line), flush=True)
     return 0
@@ -504,6 +523,9 @@ def run_ours(args, ws, rank, local):
         rate, k, el = cpu_oracle_rate(n, args.cpu_steps, threads)
         cpu = {"value": rate, "unit": "cell-updates/s", "cores": threads, "kind": "port",
                "sample": f"{k} SSP-RK3 steps of the {n}x{n} Sedov IC from t=0 (CPU oracle, OpenMP)"}
+        # the serial reference's stand-in: the same oracle on one thread, one step
+        rate1, k1, _ = cpu_oracle_rate(n, 1, 1)
+        cpu["serial"] = {"value": rate1, "cores": 1, "sample": f"{k1} SSP-RK3 step of the same IC, 1 thread"}
 
     line = {
         "metric": "FP64 cell-updates/s", "value": value, "unit": "cell-updates/s", "n_gpus": ws, "steps": done,
