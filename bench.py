@@ -381,6 +381,31 @@ def run_final(args):
     return 0
 
 
+def run_final_reference(args):
+    """The CPU oracle (all host cores) on the same whole run as run_final."""
+    import numpy as np
+    import __graft_entry__ as ge
+    O = ge.import_oracle()
+    O.build()
+    threads = os.cpu_count() or 1
+    O.set_threads(threads)
+    icname, lf, nf, lx, ly, bc, tfinal = FINAL_CASES[args.case]
+    lf = lf or args.n
+    nf = nf or args.n
+    p = O.make_params(lf, nf, lx=lx, ly=ly, bc=bc, tmax=tfinal)
+    U = O.initial_condition(p, icname)
+    st = O.Stepper(p)
+    t0 = time.perf_counter()
+    t, k = st.run(U, 0.0, 1 << 30)
+    el = time.perf_counter() - t0
+    print(json.dumps({"impl": "reference", "metric": "time to t_final", "case": args.case,
+                      "workload": f"{icname} {lf}x{nf}, BC {bc}, t_final={tfinal} (CPU oracle, OpenMP)",
+                      "steps": k, "t": t, "seconds": el, "value": lf * nf * k / el, "unit": "cell-updates/s",
+                      "cores": threads, "final_state": {"sum_rho": float(U[4:-4, 4:-4, 0].sum()),
+                                                        "sum_E": float(U[4:-4, 4:-4, 3].sum())}}), flush=True)
+    return 0
+
+
 def run_reference(args, ws, rank):
     if rank != 0:
         return 0
@@ -553,7 +578,10 @@ def main():
     args = parse()
     ws, rank, local = dist_setup(args)
     if args.final:
-        rc = run_final(args) if rank == 0 else 0
+        if rank != 0:
+            rc = 0
+        else:
+            rc = run_final_reference(args) if args.impl == "reference" else run_final(args)
     elif args.impl == "reference":
         rc = run_reference(args, ws, rank)
     else:
