@@ -43,7 +43,7 @@ def _jobs() -> list[tuple[list[str], Path]]:
                         ("stage_fast", ["-DGPM_EXACT=0", "--fmad=true"])):
         obj = BUILD / f"{name}.o"
         jobs.append(([nvcc, *common, *flags, "-c", str(CSRC / "stage_kernels.cu"), "-o", str(obj)], obj))
-    for src in ("nn_gate.cu", "probe.cu", "noalloc.cu", "adjoint.cu"):
+    for src in ("nn_gate.cu", "nn_ref.cu", "probe.cu", "noalloc.cu", "adjoint.cu"):
         obj = BUILD / (Path(src).stem + ".o")
         jobs.append(([nvcc, *common, "-c", str(CSRC / src), "-o", str(obj)], obj))
     gxx = shutil.which("g++") or "g++"

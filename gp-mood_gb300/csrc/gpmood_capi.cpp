@@ -16,6 +16,7 @@
 #include "../../include/gpmood.h"
 #include "gpm_common.h"
 #include "nn_gate.h"
+#include "nn_ref.h"
 
 struct gpmood_ctx {
     gpmood_params p;
@@ -40,6 +41,7 @@ struct gpmood_ctx {
     bool dt_pending;              // dSc->dtmin_bits holds Setdt of dU
     gpmood_counters ctr;
     NnGate* nn;                   // a-priori gate and training kernels
+    NnRef* nnref;                 // the reference's own network (nn_reference = 1)
     int8_t* dStageOrd;            // CellGPO at the end of each RK stage (GPM_MAXST x ncell)
     int nstages;                  // Forward_Euler calls per step: FE 1, SSP-RK2 2, SSP-RK3 3, SSP-RK4 5
     double* dRk4[5];              // SSP-RK4 work arrays U3, U4, FU3, FU4, Fl (U1, U2 are dU1, dU2)
@@ -114,25 +116,33 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, int bc_stage)
     cudaEvent_t* ev = c->ev[stage];
     c->kt->bc(c->g, uin, c->dSc, bc_stage, s);  // Boundary_C(Uin), :64
     c->ctr.kernel_launches += 2;
-    bool uniform = true;
+    bool uniform = true, fixup = false, nnref = false;
     CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, s));  // CellGPO = mord, :48
     CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), s));
-    if (c->p.method == GPMOOD_NN_GP_MOOD && c->niter + 1 > c->p.nsteps_with_no_nn) {
-        // gated cells start at mord-2 (:51-56) and are listed in tlist[1]
-        int rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1], s);
+    if (c->p.method == GPMOOD_NN_GP_MOOD && c->niter + 1 > c->p.nsteps_with_no_nn) {  // :51-56
+        int rc;
+        if (c->p.nn_reference) {  // the reference's network sets every CellGPO to 1 or 3
+            rc = nn_ref_orders(c->nnref, c->g, uin, c->dOrder, &c->dSc->apriori_step, nullptr, s);
+            nnref = true;
+        } else {  // gated cells start at mord-2 and are listed in tlist[1]
+            rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1], s);
+            fixup = true;
+        }
         if (rc < 0) return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
         c->ctr.kernel_launches += rc;
         uniform = false;
     }
     StageArgs a = stage_args(c, uin, uout, stage, uniform);
+    if (nnref) a.g.dmp = 0;  // NN_DETECTION: NaN and positivity only (mod_subroutine_NN_MOOD.f90:22-35)
     if (c->timing) cudaEventRecord(ev[0], s);
     // First pass over every face at mord; the faces of gated cells are then
     // recomputed at min(CellGPO) of their two cells, which gives every stored
-    // flux the value of a first pass at the gated orders.
+    // flux the value of a first pass at the gated orders.  The reference's
+    // network sets every order, so its first pass reads them face by face.
     StageArgs au = a;
-    au.uniform_order = 1;
+    au.uniform_order = nnref ? 0 : 1;
     c->flux_nl[stage] = kt.flux_all(au, c->w, s);
-    if (!uniform) {
+    if (fixup) {
         kt.mood_faces(a, c->w, 1, c->p.lf * c->p.nf, s);
         c->ctr.kernel_launches += 1;
     }
@@ -322,6 +332,8 @@ int validate(const gpmood_params* p, char* why, size_t n) {
     if (!(p->cfl > 0) || !(p->lx > 0) || !(p->ly > 0) || !(p->ell_o_dx > 0)) { snprintf(why, n, "CFL, Lx, Ly, ell_o_dx must be > 0"); return -1; }
     if (p->fp_mode != GPMOOD_FP_EXACT && p->fp_mode != GPMOOD_FP_FAST) { snprintf(why, n, "fp_mode %d unknown", p->fp_mode); return -1; }
     if (p->max_mood_iters < 0) { snprintf(why, n, "max_mood_iters must be >= 0 (0: no cap but termination)"); return -1; }
+    if (p->nn_reference && p->mord != 3 && p->mord != 5) {
+        snprintf(why, n, "nn_reference needs Mord 3 or 5 (the R+1 stencil of the reference's network)"); return -1; }
     return 0;
 }
 
@@ -335,6 +347,7 @@ void free_all(gpmood_ctx* c) {
     if (c->hSc) cudaFreeHost(c->hSc);
     if (c->hCount) cudaFreeHost(c->hCount);
     if (c->nn) nn_gate_destroy(c->nn);
+    if (c->nnref) nn_ref_destroy(c->nnref);
     for (int st = 0; st < GPM_MAXST; st++)
         for (int i = 0; i < 4; i++)
             if (c->ev[st][i]) cudaEventDestroy(c->ev[st][i]);
@@ -476,7 +489,8 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
         return GPMOOD_E_CUDA;
     }
     c->nn = nn_gate_create(c->g);
-    if (!c->nn) {
+    c->nnref = nn_ref_create();
+    if (!c->nn || !c->nnref) {
         fail(c, GPMOOD_E_CUDA, "NN gate allocation failed");
         free_all(c);
         delete c;
@@ -649,8 +663,8 @@ int gpmood_get_orders(gpmood_ctx* c, signed char* orders) {
 int gpmood_advance(gpmood_ctx* c, int nsteps, int* steps_done) {
     if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
     if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
-    if (c->p.method == GPMOOD_NN_GP_MOOD && !nn_gate_loaded(c->nn))
-        return fail(c, GPMOOD_E_STATE, "method NN_GP_MOOD needs the gate's parameters (gpmood_set_nn)");
+    if (c->p.method == GPMOOD_NN_GP_MOOD && (c->p.nn_reference ? !nn_ref_loaded(c->nnref) : !nn_gate_loaded(c->nn)))
+        return fail(c, GPMOOD_E_STATE, "method NN_GP_MOOD needs the network's parameters (gpmood_set_nn)");
     if (steps_done) *steps_done = 0;
     int done = 0;
     while (done < nsteps && c->t < c->p.tmax && c->niter < c->p.nmax) {  // main.f90:145
@@ -718,8 +732,28 @@ int gpmood_fast_rcp(const double* d_x, double* d_y, int n) {
 
 int gpmood_set_nn(gpmood_ctx* c, const float* params, int n) {
     if (!c || !params) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    if (c->p.nn_reference) {
+        const int rc = nn_ref_set(c->nnref, params, n, c->p.mord, c->stream);
+        if (rc == -1)
+            return fail(c, GPMOOD_E_ARG, "%d values is no reference network for Mord %d (len^2 + (L+4) len + 2, L = %d)",
+                        n, c->p.mord, nn_ref_inputs(c->p.mord));
+        if (rc) return fail(c, GPMOOD_E_CUDA, "reference network upload failed");
+        CU(cudaStreamSynchronize(c->stream));
+        return 0;
+    }
     if (n != NN_GATE_NPARAMS) return fail(c, GPMOOD_E_ARG, "expected %d gate parameters, got %d", NN_GATE_NPARAMS, n);
     if (nn_gate_set(c->nn, params, c->stream)) return fail(c, GPMOOD_E_CUDA, "NN gate upload failed");
+    CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
+int gpmood_nn_ref_logits(gpmood_ctx* c, float* d_logits) {
+    if (!c || !d_logits) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
+    if (!c->p.nn_reference || !nn_ref_loaded(c->nnref)) return fail(c, GPMOOD_E_STATE, "no reference network loaded");
+    CU(cudaMemsetAsync(&c->dSc->apriori_step, 0, sizeof(unsigned long long), c->stream));
+    if (nn_ref_orders(c->nnref, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, d_logits, c->stream) < 0)
+        return fail(c, GPMOOD_E_CUDA, "reference network: %s", cudaGetErrorString(cudaGetLastError()));
     CU(cudaStreamSynchronize(c->stream));
     return 0;
 }
@@ -733,12 +767,15 @@ int gpmood_set_nn_threshold(gpmood_ctx* c, float thr) {
 int gpmood_nn_predict(gpmood_ctx* c, signed char* gated, long long* n_gated) {
     if (!c || !gated) return fail(c, GPMOOD_E_ARG, "NULL argument");
     if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
-    if (!nn_gate_loaded(c->nn)) return fail(c, GPMOOD_E_STATE, "no gate parameters (gpmood_set_nn)");
+    const bool ref = c->p.nn_reference != 0;
+    if (ref ? !nn_ref_loaded(c->nnref) : !nn_gate_loaded(c->nn))
+        return fail(c, GPMOOD_E_STATE, "no network parameters (gpmood_set_nn)");
     CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, c->stream));
     CU(cudaMemsetAsync(&c->dSc->apriori_step, 0, sizeof(unsigned long long), c->stream));
     CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), c->stream));
-    if (nn_gate_orders(c->nn, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1],
-                       c->stream) < 0)
+    if ((ref ? nn_ref_orders(c->nnref, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, nullptr, c->stream)
+             : nn_gate_orders(c->nn, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1],
+                              c->stream)) < 0)
         return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
     CU(cudaMemcpy2DAsync(gated, (size_t)c->p.lf, c->dOrder + (size_t)GPM_NGC * c->g.nx + GPM_NGC, (size_t)c->g.nx,
                          (size_t)c->p.lf, (size_t)c->p.nf, cudaMemcpyDeviceToHost, c->stream));
@@ -746,7 +783,7 @@ int gpmood_nn_predict(gpmood_ctx* c, signed char* gated, long long* n_gated) {
     CU(cudaMemcpyAsync(&cnt, &c->dSc->apriori_step, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     const size_t nint = (size_t)c->p.lf * c->p.nf;
-    for (size_t i = 0; i < nint; i++) gated[i] = gated[i] < c->p.mord ? 1 : 0;
+    for (size_t i = 0; i < nint; i++) gated[i] = (ref ? gated[i] == 1 : gated[i] < c->p.mord) ? 1 : 0;
     if (n_gated) *n_gated = (long long)cnt;
     return 0;
 }

@@ -44,7 +44,7 @@ class Params(C.Structure):
                 ("tmax", C.c_double), ("integrator", C.c_int), ("method", C.c_int), ("mord", C.c_int),
                 ("ngp", C.c_int), ("dmp", C.c_int), ("u2", C.c_int), ("u2_tol", C.c_int), ("num_flux", C.c_int),
                 ("lf", C.c_int), ("nf", C.c_int), ("bc_type", C.c_int), ("nmax", C.c_int), ("fp_mode", C.c_int),
-                ("max_mood_iters", C.c_int), ("nsteps_with_no_nn", C.c_int)]
+                ("max_mood_iters", C.c_int), ("nsteps_with_no_nn", C.c_int), ("nn_reference", C.c_int)]
 
 
 class Counters(C.Structure):
@@ -80,6 +80,7 @@ SIGNATURES = {
     "gpmood_time_stepping_dev": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double], C.c_int),
     "gpmood_set_nn": ([C.c_void_p, C.POINTER(C.c_float), C.c_int], C.c_int),
     "gpmood_set_nn_threshold": ([C.c_void_p, C.c_float], C.c_int),
+    "gpmood_nn_ref_logits": ([C.c_void_p, C.c_void_p], C.c_int),
     "gpmood_nn_predict": ([C.c_void_p, C.POINTER(C.c_byte), C.POINTER(C.c_longlong)], C.c_int),
     "gpmood_get_stage_orders": ([C.c_void_p, C.c_int, C.POINTER(C.c_byte)], C.c_int),
     "gpmood_nn_features": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
@@ -314,6 +315,10 @@ class Solver:
     def set_nn(self, params: np.ndarray) -> None:
         a = np.ascontiguousarray(params, dtype=np.float32).ravel()
         self._check(self.lib.gpmood_set_nn(self._h, a.ctypes.data_as(C.POINTER(C.c_float)), a.size))
+
+    def nn_ref_logits(self, d_logits: int) -> None:
+        """r(1), r(2) of the reference's network for every interior cell (device array)."""
+        self._check(self.lib.gpmood_nn_ref_logits(self._h, C.c_void_p(d_logits)))
 
     def set_nn_threshold(self, logit_threshold: float) -> None:
         self._check(self.lib.gpmood_set_nn_threshold(self._h, float(logit_threshold)))

@@ -84,6 +84,10 @@ typedef struct gpmood_params {
     int max_mood_iters;   /* MOOD passes allowed per stage before GPMOOD_E_MOOD_CAP; 0 (default)
                              allows 2*lf*nf+2, more than a terminating loop can take */
     int nsteps_with_no_nn;/* gate off for the first steps (global_variables.f90:97) */
+    int nn_reference;     /* method NN_GP_MOOD: 0 the BF16 36-64-64-1 gate (default);
+                             1 the reference's own network and NN_DETECTION (mod_NN.f90:14-58,
+                             mod_subroutine_NN_MOOD.f90): FP32 sigmoid MLP on the raw R+1
+                             stencil, CellGPO 1 or 3, a-posteriori NaN/positivity checks only */
 } gpmood_params;
 
 /* Per-step and cumulative counters (global_variables.f90:71, main.f90:165-167). */
@@ -235,8 +239,16 @@ int  gpmood_fast_rcp(const double* d_x, double* d_y, int n);
 
 /* Load the 36-64-64-1 gate: w0[64][36], b0[64], w1[64][64], b1[64], w2[64], b2[1]
  * as one float array of 6593 values in that order (PyTorch flatten order, the
- * order of neural_network/save_NN_for_fortran.py:13-23). */
+ * order of neural_network/save_NN_for_fortran.py:13-23).  With nn_reference = 1
+ * the same call loads the reference's network instead: W0[len][L], b0[len],
+ * W1[len][len], b1[len], W2[2][len], b2[2] with L = 52 (Mord 3) or 100
+ * (Mord 5) and any hidden width len <= 128 (the file read by load_NN,
+ * mod_NN.f90:60-110). */
 int  gpmood_set_nn(gpmood_ctx* ctx, const float* params, int n);
+/* The reference network's two outputs r(1), r(2) of every interior cell of
+ * the device-resident state into d_logits[2*lf*nf] (0, 0 for constant
+ * stencils); nn_reference = 1 only. */
+int  gpmood_nn_ref_logits(gpmood_ctx* ctx, float* d_logits);
 /* The gate fires when the logit exceeds this value (default 0, i.e. p > 0.5). */
 int  gpmood_set_nn_threshold(gpmood_ctx* ctx, float logit_threshold);
 /* Gate decision on the device-resident state: gated[lf*nf] = 1 where the cell

@@ -21,7 +21,7 @@ module gpmood_iface
    type, bind(C) :: gpmood_params
       real(c_double) :: cfl, ell_o_dx, lx, ly, tmax
       integer(c_int) :: integrator, method, mord, ngp, dmp, u2, u2_tol, num_flux
-      integer(c_int) :: lf, nf, bc_type, nmax, fp_mode, max_mood_iters, nsteps_with_no_nn
+      integer(c_int) :: lf, nf, bc_type, nmax, fp_mode, max_mood_iters, nsteps_with_no_nn, nn_reference
    end type
 
    interface

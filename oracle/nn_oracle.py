@@ -103,3 +103,57 @@ def loss_grad(p, x, y, pos_weight=1.0, emulate_bf16=True):
     g_W0 = dh1b.T @ x64
     g = np.concatenate([g_W0.ravel(), g_b0, g_W1.ravel(), g_b1, g_w2, [g_b2]])
     return loss, g
+
+
+# ---------------------------------------------------------------------------
+# The reference's own network (mod_NN.f90:14-58,157-183, format_input of
+# mod_append_NN_dataset.f90:81-125): raw FP32 conserved variables of the R+1
+# stencil ixiy_sp1(Mord+2, :) (GP_init.f90:270-355), variable fastest; FP32
+# sigmoid MLP; r(1) > r(2) -> CellGPO 1, else 3; constant stencils -> 3.
+SP1 = [(0, 0), (-1, 0), (0, 1), (1, 0), (0, -1), (-1, -1), (-1, 1), (1, 1), (1, -1), (0, -2), (-2, 0), (0, 2), (2, 0),
+       (-3, 0), (-2, 1), (-1, 2), (0, 3), (1, 2), (2, 1), (3, 0), (2, -1), (1, -2), (0, -3), (-1, -2), (-2, -1)]
+
+
+def ref_features(U: np.ndarray, mord: int):
+    """(x [nf*lf, L] float32, constant [nf*lf] bool) of every interior cell, x fastest."""
+    npts = 13 if mord == 3 else 25
+    nf, lf = U.shape[0] - 8, U.shape[1] - 8
+    cols = []
+    for ox, oy in SP1[:npts]:
+        cols.append(U[4 + oy:4 + oy + nf, 4 + ox:4 + ox + lf].astype(np.float32).reshape(-1, 4))
+    q = np.stack(cols, axis=1)  # [cells, npts, 4]
+    span = q.max(axis=1) - q.min(axis=1)  # float32
+    const = np.all(span.astype(np.float64) < 1e-10, axis=1)
+    return q.reshape(q.shape[0], -1), const
+
+
+def ref_unpack(p: np.ndarray, L: int):
+    n = p.size
+    length = next(k for k in range(1, 129) if k * k + (L + 4) * k + 2 == n)
+    o = 0
+    W0 = p[o:o + length * L].reshape(length, L); o += length * L
+    b0 = p[o:o + length]; o += length
+    W1 = p[o:o + length * length].reshape(length, length); o += length * length
+    b1 = p[o:o + length]; o += length
+    W2 = p[o:o + 2 * length].reshape(2, length); o += 2 * length
+    b2 = p[o:o + 2]
+    return W0, b0, W1, b1, W2, b2
+
+
+def ref_forward(p: np.ndarray, x: np.ndarray):
+    """r [cells, 2] of the reference's forward in FP32, sums in index order."""
+    x = x.astype(np.float32)
+    W0, b0, W1, b1, W2, b2 = ref_unpack(np.asarray(p, np.float32), x.shape[1])
+    one = np.float32(1.0)
+
+    def layer(W, b, h):
+        s = np.zeros((h.shape[0], W.shape[0]), np.float32)
+        for j in range(W.shape[1]):
+            s = s + W[:, j][None, :] * h[:, j][:, None]
+        return s + b[None, :]
+
+    h0 = layer(W0, b0, x)
+    h0 = one / (one + np.exp(-h0))
+    h1 = layer(W1, b1, h0)
+    h1 = one / (one + np.exp(-h1))
+    return layer(W2, b2, h1)
