@@ -1,6 +1,6 @@
 // nn_ref.cu -- the reference's own a-priori network (method NN_GP_MOOD with
 // gpmood_params.nn_reference = 1): compute_CellGPO_with_NN, format_input and
-// forward of gp-mood-code/mod_NN.f90:14-58,157-183 and
+// forward of gp-mood-code/mod_NN.f90:14-58,168-183 and
 // mod_append_NN_dataset.f90:81-125.
 //
 // Per interior cell: the conserved variables of the R+1 stencil
