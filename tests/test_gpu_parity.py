@@ -19,6 +19,11 @@ CASES = {
     "dmr": ("dmr", 96, 24, dict(bc=35, lx=4.0, ly=1.0, tmax=0.2)),
     "vortex": ("vortex", 48, 48, dict(bc=18, lx=10.0, ly=10.0, tmax=1.0)),
     "rp2d3_r1": ("rp2d3", 64, 64, dict(bc=17, tmax=0.8, mord=3, ngp=2)),
+    # ragged sizes: no dimension a multiple of the 32x8 face tile
+    "ragged": ("rp2d3", 37, 19, dict(bc=17, tmax=0.8)),
+    "ragged_periodic": ("vortex", 33, 41, dict(bc=18, lx=10.0, ly=10.0, tmax=1.0)),
+    # smaller than one tile in both directions
+    "tiny": ("rp2d3", 8, 6, dict(bc=17, tmax=0.8)),
 }
 
 
@@ -67,7 +72,7 @@ def test_exact_mode_bitwise(pkg, oracle, case):
         assert nan_equal(Ugr, Ur), f"state differs at step {step}: max |d| = {np.nanmax(np.abs(Ugr - Ur))}"
 
 
-@pytest.mark.parametrize("case", ["rp2d3", "sedov", "vortex", "dmr"])
+@pytest.mark.parametrize("case", ["rp2d3", "sedov", "vortex", "dmr", "ragged", "tiny"])
 def test_fast_mode_tolerance(pkg, oracle, case):
     ic, lf, nf, kn = CASES[case]
     p = _oracle_params(oracle, lf, nf, kn)

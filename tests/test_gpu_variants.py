@@ -24,6 +24,12 @@ VARIANTS = {
     "rk4": (12, 100, 5, 3),
     "shipped_2drp3": (10, 103, 3, 2),  # problems/2DRP3_GPMOOD.f90: Mord 3, ngp 2, unsplit
     "rk4_hll": (12, 102, 5, 3),
+    # Gauss points per face 1, 2, 4, 5 (GP_init.f90:45-83) and the first-order method
+    "ngp1": (10, 100, 5, 1),
+    "ngp2": (10, 100, 5, 2),
+    "ngp4": (10, 100, 5, 4),
+    "ngp5": (10, 100, 5, 5),
+    "mord1": (10, 100, 1, 1),
 }
 
 
@@ -55,7 +61,7 @@ def test_variant_exact_mode_bitwise(pkg, oracle, name):
         assert nan_equal(Ugr, Ur), (step, np.nanmax(np.abs(Ugr - Ur)))
 
 
-@pytest.mark.parametrize("name", ["unsplit", "rk4", "hll"])
+@pytest.mark.parametrize("name", ["unsplit", "rk4", "hll", "ngp2", "ngp5"])
 def test_variant_fast_mode_tolerance(pkg, oracle, name):
     for step, dt, dtg, Ur, Ugr in _run(pkg, oracle, name, pkg.FP_FAST):
         pass
