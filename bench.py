@@ -58,7 +58,7 @@ def parse():
     ap.add_argument("--adjoint", type=int, default=1, help="also time the adjoint form (0: skip)")
     ap.add_argument("--final", action="store_true",
                     help="run plain (and NN-gated unless --nn 0) GP-MOOD from t=0 to t_final and compare them")
-    ap.add_argument("--case", choices=("sedov", "rp2d3", "dmr"), default="sedov",
+    ap.add_argument("--case", choices=("sedov", "rp2d3", "dmr", "dmr_1024x256"), default="sedov",
                     help="problem of --final: Sedov n^2 (t_final 0.05), 2DRP3 256^2 (0.8), DMR 4096x1024 (0.2)")
     return ap.parse_args()
 
@@ -322,6 +322,7 @@ FINAL_CASES = {
     "sedov": ("sedov", None, None, 1.0, 1.0, 20, TMAX),
     "rp2d3": ("rp2d3", 256, 256, 1.0, 1.0, 17, 0.8),
     "dmr": ("dmr", 4096, 1024, 4.0, 1.0, 35, 0.2),
+    "dmr_1024x256": ("dmr", 1024, 256, 4.0, 1.0, 35, 0.2),
 }
 
 
@@ -369,6 +370,8 @@ def run_final(args):
                      "unit": "cell-updates/s", "detected_total": c.detected_total,
                      "max_passes_stage": c.max_passes_stage, "status_flags": c.status_flags,
                      "flux_share": tm.flux_ms / ms if ms else None, "mood_share": tm.mood_ms / ms if ms else None,
+                     "mood_passes": tm.mood_passes,
+                     "us_per_mood_pass": tm.mood_ms * 1e3 / tm.mood_passes if tm.mood_passes else None,
                      "final_state": {"sum_rho": float(U[4:-4, 4:-4, 0].sum()), "sum_E": float(U[4:-4, 4:-4, 3].sum())}}
     if args.nn:
         out["nn_gated"]["speedup_vs_plain"] = out["plain"]["seconds"] / out["nn_gated"]["seconds"]

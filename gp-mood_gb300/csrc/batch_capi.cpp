@@ -112,6 +112,7 @@ BatchArgs make_args(gpmood_batch* b, const double* uin, double* uout, int stage)
     a.npblocks = b->npb;
     a.stage = stage;
     a.tile = b->tile;
+    a.mood_solo = gpm_mood_solo_default();
     return a;
 }
 

@@ -50,6 +50,7 @@ struct BatchArgs {
     int npblocks;
     int stage;            // 0, 1, 2 -> t_rk = t, t+dt, t+dt/2
     int tile;             // face-tile shape index chosen by the autotuner
+    int mood_solo;        // as GridGeom::mood_solo
 };
 
 // Face-tile shapes (TX x TY faces per CTA) the autotuner chooses from.  The

@@ -73,7 +73,12 @@ struct GridGeom {
     int bc_type, ngp, mord, method;
     int dmp, u2, u2_tol;
     int num_flux;        // 100 HLLC, 101 LLF, 102 HLL, 103 unsplit
+    int mood_solo;       // device MOOD loop: lists of at most this many cells run in one CTA
 };
+
+// Default of GridGeom::mood_solo; the environment variable GPMOOD_MOOD_SOLO
+// overrides it (tuning only: results do not depend on it).
+int gpm_mood_solo_default();
 
 // Scalars that stay on the device across a step.
 struct DevScalars {

@@ -61,6 +61,14 @@ struct gpmood_ctx {
 double gpm_probe_fp64();
 int gpm_fast_rcp_dev(const double* x, double* y, int n);
 
+int gpm_mood_solo_default() {
+    static const int v = [] {
+        const char* e = getenv("GPMOOD_MOOD_SOLO");
+        return e && *e ? atoi(e) : 12;
+    }();
+    return v;
+}
+
 namespace {
 
 thread_local char g_err[512];
@@ -285,6 +293,7 @@ int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
             c->tm.update_ms += u_;
             c->tm.update_launches += 1;
             c->tm.mood_ms += m;
+            c->tm.mood_passes += np - 1;
         }
     }
     c->ctr.detected_last_step = (long long)c->hSc->detected_step;
@@ -404,6 +413,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     c->g.mord = p->mord;
     c->g.method = p->method;
     c->g.num_flux = p->num_flux;
+    c->g.mood_solo = gpm_mood_solo_default();
     c->nstages = p->integrator == GPMOOD_FE ? 1 : p->integrator == GPMOOD_SSP_RK2 ? 2 : p->integrator == GPMOOD_SSP_RK4 ? 5 : 3;
     c->g.dmp = p->dmp;
     c->g.u2 = p->u2;

@@ -69,28 +69,31 @@ __host__ __device__ constexpr int st_oy(int m) {
 }
 __host__ __device__ constexpr int np_of(int ord) { return ord == 1 ? 1 : (ord == 3 ? 5 : 13); }
 
-// GP reconstruction of one face of one cell at NGP Gauss points:
-// u[g][k] = sum_m zt[g][m] * q[m][k], sequential in m (mod_GP_MOOD.f90:61).
+// GP reconstruction of one face of one cell at one Gauss point (weights z):
+// u[k] = sum_m z[m] * q[m][k], sequential in m (mod_GP_MOOD.f90:61).
+template <int NP>
+__device__ __forceinline__ void gp_recon_at(const double* __restrict__ z, const Cell* q, double* u) {
+    double s0 = z[0] * q[0].r, s1 = z[0] * q[0].mx, s2 = z[0] * q[0].my, s3 = z[0] * q[0].e;
+#pragma unroll
+    for (int m = 1; m < NP; m++) {
+        const double zm = z[m];
+        s0 = s0 + zm * q[m].r;
+        s1 = s1 + zm * q[m].mx;
+        s2 = s2 + zm * q[m].my;
+        s3 = s3 + zm * q[m].e;
+    }
+#if GPM_EXACT
+    u[0] = plus_zero(s0); u[1] = plus_zero(s1); u[2] = plus_zero(s2); u[3] = plus_zero(s3);
+#else
+    u[0] = s0; u[1] = s1; u[2] = s2; u[3] = s3;
+#endif
+}
+
+// ... and at all NGP Gauss points of the face (zface: NGP rows of 13).
 template <int NP, int NGP>
 __device__ __forceinline__ void gp_recon(const double* __restrict__ zface, const Cell* q, double (*u)[4]) {
 #pragma unroll
-    for (int g = 0; g < NGP; g++) {
-        const double* z = zface + g * 13;
-        double s0 = z[0] * q[0].r, s1 = z[0] * q[0].mx, s2 = z[0] * q[0].my, s3 = z[0] * q[0].e;
-#pragma unroll
-        for (int m = 1; m < NP; m++) {
-            const double zm = z[m];
-            s0 = s0 + zm * q[m].r;
-            s1 = s1 + zm * q[m].mx;
-            s2 = s2 + zm * q[m].my;
-            s3 = s3 + zm * q[m].e;
-        }
-#if GPM_EXACT
-        u[g][0] = plus_zero(s0); u[g][1] = plus_zero(s1); u[g][2] = plus_zero(s2); u[g][3] = plus_zero(s3);
-#else
-        u[g][0] = s0; u[g][1] = s1; u[g][2] = s2; u[g][3] = s3;
-#endif
-    }
+    for (int g = 0; g < NGP; g++) gp_recon_at<NP>(zface + g * 13, q, u[g]);
 }
 
 #if !GPM_EXACT

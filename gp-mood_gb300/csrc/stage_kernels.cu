@@ -579,28 +579,104 @@ __device__ __forceinline__ void face_global(const GridGeom& g, const GpWeights& 
     quad_flux<DIR, NGP>(uL, uR, w.gw, F, g.num_flux);
 }
 
-template <int DIR, int NGP>
-__device__ __forceinline__ void face_any_order(const StageArgs& a, const GpWeights& w, size_t c0) {
+// The MOOD face phase, split by Gauss point.  A pass's face list is short
+// (the faces of the cells lowered in the previous pass), so the SMs hold one
+// or two warps each and a pass waits on one warp's chain of dependent FP64
+// instructions.  NGP consecutive lanes share a face: each reconstructs both
+// sides at its own Gauss point (gp_recon_at, the per-point sum of
+// mod_GP_MOOD.f90:61) and solves that point's Riemann problem; the face's
+// lanes gather the NGP fluxes by shuffles and sum them in Gauss-point order
+// with quad_flux's expression, and the first lane stores the face.  The chain
+// is one Gauss point's work instead of the face's.  A listed cell was lowered
+// when it was listed, so its faces are at order <= 3; the 13-point branch only
+// keeps the function total.
+struct FaceGp {
+    double F[4];        // this lane's Gauss-point flux
+    double* out;        // the face's stored flux
+    const double* gw;   // Gauss weights
+};
+
+template <int DIR, int NP>
+__device__ __forceinline__ void face_gp_global(const GridGeom& g, const GpWeights& w, int o,
+                                               const double* __restrict__ uin, size_t c0, int gp, double* F) {
+    constexpr int FL = DIR == 0 ? 2 : 1;
+    constexpr int FH = DIR == 0 ? 0 : 3;
+    const ptrdiff_t row = g.nx;
+    const size_t c1 = DIR == 0 ? c0 + 1 : c0 + g.nx;
+    double uL[4], uR[4];
+    {
+        Cell q[NP];
+#pragma unroll
+        for (int m = 0; m < NP; m++) q[m] = ld_cell(uin + 4 * (c0 + st_ox(m) + row * st_oy(m)));
+        gp_recon_at<NP>(&w.zt[o][FL][gp][0], q, uL);
+    }
+    {
+        Cell q[NP];
+#pragma unroll
+        for (int m = 0; m < NP; m++) q[m] = ld_cell(uin + 4 * (c1 + st_ox(m) + row * st_oy(m)));
+        gp_recon_at<NP>(&w.zt[o][FH][gp][0], q, uR);
+    }
+    riemann<DIR>(g.num_flux, uL, uR, F);
+}
+
+template <int DIR>
+__device__ __forceinline__ void face_gp_any(const StageArgs& a, const GpWeights& w, size_t c0, int gp, FaceGp& f) {
     const GridGeom& g = a.g;
     const size_t c1 = DIR == 0 ? c0 + 1 : c0 + g.nx;
     const int o = min((int)a.order[c0], (int)a.order[c1]);
-    double F[4];
-    if (o >= 5) face_global<DIR, 13, NGP>(g, w, 2, a.uin, c0, F);
-    else if (o >= 3) face_global<DIR, 5, NGP>(g, w, 1, a.uin, c0, F);
-    else face_global<DIR, 1, NGP>(g, w, 0, a.uin, c0, F);
-    st_cell((DIR == 0 ? a.fx : a.fy) + 4 * c0, Cell{F[0], F[1], F[2], F[3]});
+    if (o >= 5) face_gp_global<DIR, 13>(g, w, 2, a.uin, c0, gp, f.F);
+    else if (o >= 3) face_gp_global<DIR, 5>(g, w, 1, a.uin, c0, gp, f.F);
+    else face_gp_global<DIR, 1>(g, w, 0, a.uin, c0, gp, f.F);
+    f.out = (DIR == 0 ? a.fx : a.fy) + 4 * c0;
+    f.gw = w.gw;
+}
+
+// Faces 0 .. nf-1 dealt to whole warps (stid: pack_tid, gstride: threads of
+// the grid); item(i, gp, f) fills face i's Gauss point gp.  Every lane of a
+// warp runs the same trip count, so the shuffles see full warps.
+template <int NGP, class Item>
+__device__ __forceinline__ void face_phase_gp(int nf, int stid, int gstride, Item item) {
+    constexpr int FPW = 32 / NGP;  // faces per warp
+    const int lane = threadIdx.x & 31, fl = lane / NGP, gp = lane - fl * NGP, lead = lane - gp;
+    for (int wb = (stid >> 5) * FPW; wb < nf; wb += (gstride >> 5) * FPW) {
+        const int i = wb + fl;
+        const bool act = fl < FPW && i < nf;
+        FaceGp f;
+        f.F[0] = f.F[1] = f.F[2] = f.F[3] = 0.0;
+        f.out = nullptr;
+        f.gw = nullptr;
+        if (act) item(i, gp, f);
+        double acc[4];
+#pragma unroll
+        for (int j = 0; j < NGP; j++) {
+            const int src = min(lead + j, 31);
+            const double wj = act ? f.gw[j] : 0.0;
+#pragma unroll
+            for (int k = 0; k < 4; k++) {
+                const double v = __shfl_sync(0xffffffffu, f.F[k], src);
+                acc[k] = (j == 0) ? v * wj : acc[k] + v * wj;
+            }
+        }
+        if (act && gp == 0) {
+#if GPM_EXACT
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc[k] = plus_zero(acc[k]);
+#endif
+            st_cell(f.out, Cell{acc[0], acc[1], acc[2], acc[3]});
+        }
+    }
 }
 
 template <int NGP>
 __global__ void __launch_bounds__(128) k_mood_faces(StageArgs a, const __grid_constant__ GpWeights w, int cur) {
     const int nt = a.sc->ntrb[cur];
     // 4 faces per troubled cell: x faces (l-1,n), (l,n), y faces (l,n-1), (l,n)
-    for (int i = pack_tid(); i < 4 * nt; i += gridDim.x * blockDim.x) {
+    face_phase_gp<NGP>(4 * nt, pack_tid(), gridDim.x * blockDim.x, [&](int i, int gp, FaceGp& f) {
         int dir, side;
         const size_t c = (size_t)a.tlist[cur][face_item(i, nt, &dir, &side)];
-        if (dir == 0) face_any_order<0, NGP>(a, w, side == 0 ? c - 1 : c);
-        else face_any_order<1, NGP>(a, w, side == 0 ? c - a.g.nx : c);
-    }
+        if (dir == 0) face_gp_any<0>(a, w, side == 0 ? c - 1 : c, gp, f);
+        else face_gp_any<1>(a, w, side == 0 ? c - a.g.nx : c, gp, f);
+    });
 }
 
 __global__ void __launch_bounds__(256) k_mood_cells(StageArgs a, const __grid_constant__ GpWeights w, int cur,
@@ -639,8 +715,9 @@ __global__ void __launch_bounds__(256) k_mood_cells(StageArgs a, const __grid_co
 
 // ---------------------------------------------------------------------------
 // The whole MOOD loop on the device: one cooperative launch runs passes 2, 3,
-// ... until the troubled list is empty, with grid barriers between the three
-// phases of a pass (cascade, faces, crosses).  Every CTA is co-resident
+// ... until the troubled list is empty, with a grid barrier after each of the
+// two phases of a pass (faces, crosses; the cascade is applied when a cell is
+// listed).  Every CTA is co-resident
 // (cooperative launch), so the barrier cannot wait on an unscheduled CTA; its
 // spin is still bounded, and a timeout records GPM_STATUS_BARRIER and makes
 // every CTA leave.
@@ -675,6 +752,21 @@ __device__ __forceinline__ bool grid_sync(GridBar* b) {
     return *(volatile int*)&b->err == 0;
 }
 
+// Passes whose troubled list holds at most GridGeom::mood_solo cells run in CTA 0
+// alone, with CTA barriers: such a pass is a few dependent chains of FP64
+// work, and two grid barriers cost more than its work.  Every CTA reads the
+// same count after a grid barrier, so all take the switch at the same pass;
+// the others leave and CTA 0 runs the loop to its end (a list that grows
+// again is still done, by one CTA's threads).  Runs whose cascade crawls
+// cell by cell need hundreds of such passes per stage.
+__device__ __forceinline__ bool mood_sync(GridBar* b, bool solo) {
+    if (solo) {
+        __syncthreads();
+        return true;
+    }
+    return grid_sync(b);
+}
+
 template <int NGP>
 __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, const __grid_constant__ GpWeights w, GridBar* bar,
                                                       int max_pass, int stage) {
@@ -682,7 +774,8 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
     const double qx = a.sc->qx, qy = a.sc->qy;
     const unsigned epoch = a.sc->stamp_epoch;  // stamps epoch+2, epoch+3, ... are new
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
-    const int stid = pack_tid();  // whole warps of work items, dealt over all SMs
+    int stid = pack_tid(), wstride = gstride;  // whole warps of work items, dealt over all SMs
+    bool solo = false;
     int cur = 0, pass = 1;  // pass 1 (all faces) ran before this kernel
     for (;;) {
         const int nt = *(volatile int*)&a.sc->ntrb[cur];
@@ -691,6 +784,12 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
             if (gtid == 0) a.sc->status |= GPM_STATUS_MOODCAP;
             break;
         }
+        if (!solo && nt <= g.mood_solo) {
+            if (blockIdx.x != 0) return;
+            solo = true;
+            stid = threadIdx.x;
+            wstride = blockDim.x;
+        }
         pass++;
         // the listed cells' orders were lowered when they were listed
         if (gtid == 0) {
@@ -698,18 +797,18 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
             a.sc->detected_step += (unsigned long long)nt;
         }
         // the four faces of every troubled cell at the new orders
-        for (int i = stid; i < 4 * nt; i += gstride) {
+        face_phase_gp<NGP>(4 * nt, stid, wstride, [&](int i, int gp, FaceGp& f) {
             int dir, side;
             const size_t c = (size_t)a.tlist[cur][face_item(i, nt, &dir, &side)];
-            if (dir == 0) face_any_order<0, NGP>(a, w, side == 0 ? c - 1 : c);
-            else face_any_order<1, NGP>(a, w, side == 0 ? c - g.nx : c);
-        }
-        if (!grid_sync(bar)) return;
+            if (dir == 0) face_gp_any<0>(a, w, side == 0 ? c - 1 : c, gp, f);
+            else face_gp_any<1>(a, w, side == 0 ? c - g.nx : c, gp, f);
+        });
+        if (!mood_sync(bar, solo)) return;
         // the 5-point crosses: Uout from Uin and the current fluxes, DETECTION
         const unsigned pid = epoch + (unsigned)pass;
         const int nxt = cur ^ 1, total = 5 * nt;
-        const int lim = ((total + gstride - 1) / gstride) * gstride;
-        for (int base = 0; base < lim; base += gstride) {
+        const int lim = ((total + wstride - 1) / wstride) * wstride;
+        for (int base = 0; base < lim; base += wstride) {
             const int i = base + stid;
             bool trb = false;
             int cval = 0;
@@ -728,7 +827,7 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
             if (trb) cascade_order(&a.order[cval]);
             list_append(trb, a.tlist[nxt], &a.sc->ntrb[nxt], cval);
         }
-        if (!grid_sync(bar)) return;
+        if (!mood_sync(bar, solo)) return;
         cur ^= 1;
     }
     if (gtid == 0) {  // every CTA read the epoch before the first barrier
@@ -945,6 +1044,7 @@ __device__ __forceinline__ GridGeom bgeom(const BatchArgs& a, const BProb& p) {
     g.dx = p.dx; g.dy = p.dy;
     g.bc_type = a.bc_type; g.ngp = a.ngp; g.mord = a.mord; g.method = a.method;
     g.dmp = a.dmp; g.u2 = a.u2; g.u2_tol = a.u2_tol; g.num_flux = a.num_flux;
+    g.mood_solo = a.mood_solo;
     return g;
 }
 
@@ -1173,6 +1273,23 @@ void blaunch_update(const BatchArgs& a, cudaStream_t s) {
 // One MOOD pass over every problem's list: cascade, the troubled cells' faces,
 // then their 5-point crosses.  Each kernel returns at once on an empty list,
 // so a captured graph holds a fixed number of passes at almost no cost.
+// Face i of the batch's face list at Gauss point gp (face_phase_gp item).
+__device__ __forceinline__ void kb_face_gp(const BatchArgs& a, int cur, int nt, int i, int gp, FaceGp& f) {
+    int dir, side;
+    const int2 e = a.tlist[cur][face_item(i, nt, &dir, &side)];
+    const BProb P = a.prob[e.x];
+    StageArgs sa;
+    sa.g = bgeom(a, P);
+    sa.uin = a.uin + 4 * P.off;
+    sa.fx = a.fx + 4 * P.off;
+    sa.fy = a.fy + 4 * P.off;
+    sa.order = a.order + P.off;
+    const GpWeights& w = a.wtab[P.wc];
+    const size_t c = (size_t)e.y;
+    if (dir == 0) face_gp_any<0>(sa, w, side == 0 ? c - 1 : c, gp, f);
+    else face_gp_any<1>(sa, w, side == 0 ? c - sa.g.nx : c, gp, f);
+}
+
 __global__ void kb_mood_mark(BatchArgs a, int cur) {  // the listed cells' orders are already lowered
     const int nt = a.ntrb[cur];
     if (nt == 0) return;
@@ -1185,21 +1302,8 @@ __global__ void kb_mood_mark(BatchArgs a, int cur) {  // the listed cells' order
 template <int NGP>
 __global__ void __launch_bounds__(128) kb_mood_faces(BatchArgs a, int cur) {
     const int nt = a.ntrb[cur];
-    for (int i = pack_tid(); i < 4 * nt; i += gridDim.x * blockDim.x) {
-        int dir, side;
-        const int2 e = a.tlist[cur][face_item(i, nt, &dir, &side)];
-        const BProb P = a.prob[e.x];
-        StageArgs sa;
-        sa.g = bgeom(a, P);
-        sa.uin = a.uin + 4 * P.off;
-        sa.fx = a.fx + 4 * P.off;
-        sa.fy = a.fy + 4 * P.off;
-        sa.order = a.order + P.off;
-        const GpWeights& w = a.wtab[P.wc];
-        const size_t c = (size_t)e.y;
-        if (dir == 0) face_any_order<0, NGP>(sa, w, side == 0 ? c - 1 : c);
-        else face_any_order<1, NGP>(sa, w, side == 0 ? c - sa.g.nx : c);
-    }
+    face_phase_gp<NGP>(4 * nt, pack_tid(), gridDim.x * blockDim.x,
+                       [&](int i, int gp, FaceGp& f) { kb_face_gp(a, cur, nt, i, gp, f); });
 }
 
 __global__ void __launch_bounds__(256) kb_mood_cells(BatchArgs a, int cur) {
@@ -1257,7 +1361,8 @@ void blaunch_mood_pass(const BatchArgs& a, int cur, cudaStream_t s) {
 template <int NGP>
 __global__ void __launch_bounds__(MOOD_THREADS, 1) kb_mood_loop(BatchArgs a, GridBar* bar, int max_pass) {
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
-    const int stid = pack_tid();
+    int stid = pack_tid(), wstride = gstride;
+    bool solo = false;
     int cur = 0, pass = 1;
     for (;;) {
         const int nt = *(volatile int*)&a.ntrb[cur];
@@ -1266,6 +1371,12 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) kb_mood_loop(BatchArgs a, Gri
             if (gtid == 0) a.ntrb[3] = 1;
             break;
         }
+        if (!solo && nt <= a.mood_solo) {  // as in k_mood_loop
+            if (blockIdx.x != 0) return;
+            solo = true;
+            stid = threadIdx.x;
+            wstride = blockDim.x;
+        }
         pass++;
         // the listed cells' orders were lowered when they were listed
         if (gtid == 0) {
@@ -1273,26 +1384,13 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) kb_mood_loop(BatchArgs a, Gri
             a.ntrb[2] += 1;       // stamp epoch, read after the next barrier
             a.ntrb[4] += nt;
         }
-        for (int i = stid; i < 4 * nt; i += gstride) {
-            int dir, side;
-            const int2 e = a.tlist[cur][face_item(i, nt, &dir, &side)];
-            const BProb P = a.prob[e.x];
-            StageArgs sa;
-            sa.g = bgeom(a, P);
-            sa.uin = a.uin + 4 * P.off;
-            sa.fx = a.fx + 4 * P.off;
-            sa.fy = a.fy + 4 * P.off;
-            sa.order = a.order + P.off;
-            const GpWeights& w = a.wtab[P.wc];
-            const size_t c = (size_t)e.y;
-            if (dir == 0) face_any_order<0, NGP>(sa, w, side == 0 ? c - 1 : c);
-            else face_any_order<1, NGP>(sa, w, side == 0 ? c - sa.g.nx : c);
-        }
-        if (!grid_sync(bar)) return;
+        face_phase_gp<NGP>(4 * nt, stid, wstride,
+                           [&](int i, int gp, FaceGp& f) { kb_face_gp(a, cur, nt, i, gp, f); });
+        if (!mood_sync(bar, solo)) return;
         const unsigned epoch = (unsigned)*(volatile int*)&a.ntrb[2];
         const int nxt = cur ^ 1, total = 5 * nt;
-        const int lim = ((total + gstride - 1) / gstride) * gstride;
-        for (int base = 0; base < lim; base += gstride) {
+        const int lim = ((total + wstride - 1) / wstride) * wstride;
+        for (int base = 0; base < lim; base += wstride) {
             const int i = base + stid;
             bool trb = false;
             int2 val = make_int2(0, 0);
@@ -1318,7 +1416,7 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) kb_mood_loop(BatchArgs a, Gri
             if (trb) cascade_order(a.order + a.prob[val.x].off + val.y);
             list_append2(trb, a.tlist[nxt], &a.ntrb[nxt], val);
         }
-        if (!grid_sync(bar)) return;
+        if (!mood_sync(bar, solo)) return;
         cur ^= 1;
     }
     if (gtid == 0) a.ntrb[5] = pass;

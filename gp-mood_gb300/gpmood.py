@@ -57,7 +57,7 @@ class Counters(C.Structure):
 class Timing(C.Structure):
     _fields_ = [("flux_ms", C.c_double), ("flux_launches", C.c_longlong), ("flux_faces", C.c_longlong),
                 ("update_ms", C.c_double), ("update_launches", C.c_longlong), ("mood_ms", C.c_double),
-                ("mood_faces", C.c_longlong)]
+                ("mood_passes", C.c_longlong)]
 
 
 # Every entry point of include/gpmood.h with its ctypes signature.

@@ -111,7 +111,7 @@ typedef struct gpmood_timing {
     double update_ms;        /* flux-difference update + DETECTION kernels */
     long long update_launches;
     double mood_ms;          /* MOOD passes 2, 3, ... (mark + faces + cells) */
-    long long mood_faces;    /* faces recomputed in those passes */
+    long long mood_passes;   /* passes 2, 3, ... run, all stages */
 } gpmood_timing;
 
 typedef struct gpmood_ctx gpmood_ctx;
