@@ -392,6 +392,7 @@ __device__ __forceinline__ void quad_flux(const double (*uL)[4], const double (*
 }
 
 // shock_detector, mod_subroutine_MOOD.f90:191-238, on Uin around (l, n).
+#if GPM_EXACT
 __device__ __forceinline__ bool shock_detector(const Cell& c, const Cell& L, const Cell& R, const Cell& B,
                                                const Cell& T, double dx, double dy) {
     double divV = (R.mx - L.mx) / dx + (T.my - B.my) / dy;
@@ -405,6 +406,35 @@ __device__ __forceinline__ bool shock_detector(const Cell& c, const Cell& L, con
     const double m = fmax(dx, dy);
     return (divV < -(m * m)) && (Mach > 0.2) && (gradP > 5.0);
 }
+#else
+// Fast mode: p with a supplied 1/rho.
+__device__ __forceinline__ double pressure_ir(const Cell& u, double ir) {
+    return (GPM_GAMMA - 1.) * (u.e - 0.5 * (u.mx * u.mx + u.my * u.my) * ir);
+}
+
+// Fast mode: the same three tests with six Newton reciprocals (gpm_fast_rcp)
+// in place of the nineteen IEEE divisions; the quantities agree with the
+// exact form to rounding for admissible states.  A lone warp pays ~64 cycles
+// per FP64 instruction, and a short MOOD pass waits on this chain.
+__device__ __forceinline__ bool shock_detector(const Cell& c, const Cell& L, const Cell& R, const Cell& B,
+                                               const Cell& T, double dx, double dy) {
+    const double ixy = gpm_fast_rcp(dx * dy);
+    const double idx = dy * ixy, idy = dx * ixy;
+    const double ir = gpm_fast_rcp(c.r), ir2 = ir * ir;
+    double divV = (R.mx - L.mx) * idx + (T.my - B.my) * idy;
+    divV = 0.5 * divV * ir;
+    divV = divV - 0.5 * (c.mx * (R.r - L.r) * idx + c.my * (T.r - B.r) * idy) * ir2;
+    const double Ca = 1.4 * pressure_ir(c, ir) * ir;
+    const double Mach = sqrt((c.mx * c.mx + c.my * c.my) * ir2 * gpm_fast_rcp(Ca));
+    const double rlr = gpm_fast_rcp(L.r * R.r), rbt = gpm_fast_rcp(B.r * T.r);
+    const double pL = pressure_ir(L, R.r * rlr), pR = pressure_ir(R, L.r * rlr);
+    const double pB = pressure_ir(B, T.r * rbt), pT = pressure_ir(T, B.r * rbt);
+    const double gradP = 0.5 * (fabs(pR - pL) * gpm_fast_rcp(fmin(pL, pR)) * idx +
+                                fabs(pT - pB) * gpm_fast_rcp(fmin(pB, pT)) * idy);
+    const double m = fmax(dx, dy);
+    return (divV < -(m * m)) && (Mach > 0.2) && (gradP > 5.0);
+}
+#endif
 
 // DETECTION checks for one interior cell (mod_subroutine_MOOD.f90:41-131).
 // uin points at Uin(1, l, n) of a padded array of row pitch 4*nx doubles.
@@ -413,7 +443,11 @@ __device__ __forceinline__ bool shock_detector(const Cell& c, const Cell& L, con
 __device__ __forceinline__ bool mood_troubled(const Cell& uo, const double* __restrict__ uin, int nx,
                                               const GridGeom& g, const double* d2x, const double* d2y) {
     if (le_zero_or_nan(uo.r)) return true;
+#if GPM_EXACT
     const double p = pressure(uo);
+#else
+    const double p = pressure_ir(uo, gpm_fast_rcp(uo.r));
+#endif
     if (le_zero_or_nan(p)) return true;
     if (!g.dmp) return false;
     const size_t row = (size_t)4 * nx;

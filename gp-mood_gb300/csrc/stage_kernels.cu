@@ -596,14 +596,16 @@ struct FaceGp {
     const double* gw;   // Gauss weights
 };
 
+// The two face states of one Gauss point at order NP (stencil straight from
+// global memory).
 template <int DIR, int NP>
-__device__ __forceinline__ void face_gp_global(const GridGeom& g, const GpWeights& w, int o,
-                                               const double* __restrict__ uin, size_t c0, int gp, double* F) {
+__device__ __forceinline__ void face_gp_states(const GridGeom& g, const GpWeights& w, int o,
+                                               const double* __restrict__ uin, size_t c0, int gp, double* uL,
+                                               double* uR) {
     constexpr int FL = DIR == 0 ? 2 : 1;
     constexpr int FH = DIR == 0 ? 0 : 3;
     const ptrdiff_t row = g.nx;
     const size_t c1 = DIR == 0 ? c0 + 1 : c0 + g.nx;
-    double uL[4], uR[4];
     {
         Cell q[NP];
 #pragma unroll
@@ -616,31 +618,40 @@ __device__ __forceinline__ void face_gp_global(const GridGeom& g, const GpWeight
         for (int m = 0; m < NP; m++) q[m] = ld_cell(uin + 4 * (c1 + st_ox(m) + row * st_oy(m)));
         gp_recon_at<NP>(&w.zt[o][FH][gp][0], q, uR);
     }
-    riemann<DIR>(g.num_flux, uL, uR, F);
 }
 
+// Lanes of one warp may hold faces of different orders: only the
+// reconstruction branches on the order, and the Riemann solve runs once for
+// the whole warp after the branches rejoin (an FP64 warp instruction costs
+// its SM partition ~64 cycles however many lanes are active, so a solve in
+// each branch would double the pass's critical path).
 template <int DIR>
 __device__ __forceinline__ void face_gp_any(const StageArgs& a, const GpWeights& w, size_t c0, int gp, FaceGp& f) {
     const GridGeom& g = a.g;
     const size_t c1 = DIR == 0 ? c0 + 1 : c0 + g.nx;
     const int o = min((int)a.order[c0], (int)a.order[c1]);
-    if (o >= 5) face_gp_global<DIR, 13>(g, w, 2, a.uin, c0, gp, f.F);
-    else if (o >= 3) face_gp_global<DIR, 5>(g, w, 1, a.uin, c0, gp, f.F);
-    else face_gp_global<DIR, 1>(g, w, 0, a.uin, c0, gp, f.F);
+    double uL[4], uR[4];
+    if (o >= 5) face_gp_states<DIR, 13>(g, w, 2, a.uin, c0, gp, uL, uR);
+    else if (o >= 3) face_gp_states<DIR, 5>(g, w, 1, a.uin, c0, gp, uL, uR);
+    else face_gp_states<DIR, 1>(g, w, 0, a.uin, c0, gp, uL, uR);
+    riemann<DIR>(g.num_flux, uL, uR, f.F);
     f.out = (DIR == 0 ? a.fx : a.fy) + 4 * c0;
     f.gw = w.gw;
 }
 
 // Faces 0 .. nf-1 dealt to whole warps (stid: pack_tid, gstride: threads of
-// the grid); item(i, gp, f) fills face i's Gauss point gp.  Every lane of a
-// warp runs the same trip count, so the shuffles see full warps.
+// the grid); item(i, gp, f) fills face i's Gauss point gp.  Faces 0 .. n0-1
+// (the x faces) and n0 .. nf-1 (the y faces) start on warp boundaries, so no
+// warp runs both directions' code.  Every lane of a warp runs the same trip
+// count, so the shuffles see full warps.
 template <int NGP, class Item>
-__device__ __forceinline__ void face_phase_gp(int nf, int stid, int gstride, Item item) {
+__device__ __forceinline__ void face_phase_gp(int nf, int n0, int stid, int gstride, Item item) {
     constexpr int FPW = 32 / NGP;  // faces per warp
     const int lane = threadIdx.x & 31, fl = lane / NGP, gp = lane - fl * NGP, lead = lane - gp;
-    for (int wb = (stid >> 5) * FPW; wb < nf; wb += (gstride >> 5) * FPW) {
-        const int i = wb + fl;
-        const bool act = fl < FPW && i < nf;
+    const int w0 = (n0 + FPW - 1) / FPW, nw = w0 + (nf - n0 + FPW - 1) / FPW;
+    for (int wi = stid >> 5; wi < nw; wi += gstride >> 5) {
+        const int i = wi < w0 ? wi * FPW + fl : n0 + (wi - w0) * FPW + fl;
+        const bool act = fl < FPW && i < (wi < w0 ? n0 : nf);
         FaceGp f;
         f.F[0] = f.F[1] = f.F[2] = f.F[3] = 0.0;
         f.out = nullptr;
@@ -671,7 +682,7 @@ template <int NGP>
 __global__ void __launch_bounds__(128) k_mood_faces(StageArgs a, const __grid_constant__ GpWeights w, int cur) {
     const int nt = a.sc->ntrb[cur];
     // 4 faces per troubled cell: x faces (l-1,n), (l,n), y faces (l,n-1), (l,n)
-    face_phase_gp<NGP>(4 * nt, pack_tid(), gridDim.x * blockDim.x, [&](int i, int gp, FaceGp& f) {
+    face_phase_gp<NGP>(4 * nt, 2 * nt, pack_tid(), gridDim.x * blockDim.x, [&](int i, int gp, FaceGp& f) {
         int dir, side;
         const size_t c = (size_t)a.tlist[cur][face_item(i, nt, &dir, &side)];
         if (dir == 0) face_gp_any<0>(a, w, side == 0 ? c - 1 : c, gp, f);
@@ -797,7 +808,7 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
             a.sc->detected_step += (unsigned long long)nt;
         }
         // the four faces of every troubled cell at the new orders
-        face_phase_gp<NGP>(4 * nt, stid, wstride, [&](int i, int gp, FaceGp& f) {
+        face_phase_gp<NGP>(4 * nt, 2 * nt, stid, wstride, [&](int i, int gp, FaceGp& f) {
             int dir, side;
             const size_t c = (size_t)a.tlist[cur][face_item(i, nt, &dir, &side)];
             if (dir == 0) face_gp_any<0>(a, w, side == 0 ? c - 1 : c, gp, f);
@@ -901,6 +912,7 @@ void launch_mood_cells(const StageArgs& a, const GpWeights& w, int cur, int max_
 // atomicMin on the bit pattern across CTAs (positive doubles order like their
 // bits); NaN cells are ignored (IEEE minNum, as in the CPU restatement).
 
+#if GPM_EXACT
 __device__ __forceinline__ double cell_dt(const Cell& u, double dx, double dy) {
     const double vx = u.mx / u.r;
     const double vy = u.my / u.r;
@@ -908,6 +920,17 @@ __device__ __forceinline__ double cell_dt(const Cell& u, double dx, double dy) {
     const double c = sqrt(GPM_GAMMA * p / u.r);
     return 1.0 / (1.0 / (dx / (fabs(vx) + c)) + 1.0 / (dy / (fabs(vy) + c)));
 }
+#else
+// Fast mode: dx*dy / ((|u|+c)*dy + (|v|+c)*dx) with Newton reciprocals, equal
+// to the form above up to rounding (a NaN or non-positive cell still gives NaN
+// or a non-positive value, which the reduction skips).
+__device__ __forceinline__ double cell_dt(const Cell& u, double dx, double dy) {
+    const double ir = gpm_fast_rcp(u.r);
+    const double vx = u.mx * ir, vy = u.my * ir;
+    const double c = sqrt(GPM_GAMMA * pressure_ir(u, ir) * ir);
+    return dx * dy * gpm_fast_rcp((fabs(vx) + c) * dy + (fabs(vy) + c) * dx);
+}
+#endif
 
 __device__ __forceinline__ void dt_reduce(double v, DevScalars* sc) {
 #pragma unroll
@@ -1302,7 +1325,7 @@ __global__ void kb_mood_mark(BatchArgs a, int cur) {  // the listed cells' order
 template <int NGP>
 __global__ void __launch_bounds__(128) kb_mood_faces(BatchArgs a, int cur) {
     const int nt = a.ntrb[cur];
-    face_phase_gp<NGP>(4 * nt, pack_tid(), gridDim.x * blockDim.x,
+    face_phase_gp<NGP>(4 * nt, 2 * nt, pack_tid(), gridDim.x * blockDim.x,
                        [&](int i, int gp, FaceGp& f) { kb_face_gp(a, cur, nt, i, gp, f); });
 }
 
@@ -1384,7 +1407,7 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) kb_mood_loop(BatchArgs a, Gri
             a.ntrb[2] += 1;       // stamp epoch, read after the next barrier
             a.ntrb[4] += nt;
         }
-        face_phase_gp<NGP>(4 * nt, stid, wstride,
+        face_phase_gp<NGP>(4 * nt, 2 * nt, stid, wstride,
                            [&](int i, int gp, FaceGp& f) { kb_face_gp(a, cur, nt, i, gp, f); });
         if (!mood_sync(bar, solo)) return;
         const unsigned epoch = (unsigned)*(volatile int*)&a.ntrb[2];
