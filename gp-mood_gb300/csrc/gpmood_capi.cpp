@@ -607,6 +607,32 @@ int gpmood_time_stepping(gpmood_ctx* c, const double* uin_host, double* uout_hos
     return 0;
 }
 
+int gpmood_setdt_time_stepping(gpmood_ctx* c, const double* uin_host, double* uout_host, double t, double dtfinal,
+                               double* dt_out) {
+    if (!c || !uin_host || !uout_host || !dt_out) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    CU(cudaMemcpyAsync(c->dU, uin_host, state_bytes(c), cudaMemcpyHostToDevice, c->stream));
+    c->have_state = false;  // dU no longer mirrors a set_state upload
+    c->kt->cfl(c->g, c->dU, c->dSc, c->stream);
+    c->kt->dt_finalize(c->g, c->dSc, dtfinal < 0.0 ? 0.0 : dtfinal, c->stream);
+    c->ctr.kernel_launches += 2;
+    int rc = check_launch(c, "Setdt");
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(c->hSc, c->dSc, sizeof(DevScalars), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    const double dt = c->hSc->dt;
+    *dt_out = dt;
+    c->dt_pending = false;
+    if ((c->hSc->status & GPM_STATUS_DT) || !(dt > 0) || !isfinite(dt))
+        return fail(c, GPMOOD_E_DT, "Setdt produced dt = %g", dt);
+    rc = set_time(c, t, dt);
+    if (rc) return rc;
+    rc = run_step(c, c->dU, c->dUr, false);
+    if (rc) return rc;
+    CU(cudaMemcpyAsync(uout_host, c->dUr, state_bytes(c), cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return 0;
+}
+
 int gpmood_time_stepping_dev(gpmood_ctx* c, double* d_uin, double* d_uout, double t, double dt) {
     if (!c || !d_uin || !d_uout) return fail(c, GPMOOD_E_ARG, "NULL argument");
     if (!(dt > 0) || !isfinite(dt)) return fail(c, GPMOOD_E_DT, "dt = %g", dt);

@@ -72,6 +72,7 @@ SIGNATURES = {
     "gpmood_boundary_c": ([C.c_void_p, _DP, C.c_double], C.c_int),
     "gpmood_setdt": ([C.c_void_p, _DP, C.c_double, _DP], C.c_int),
     "gpmood_time_stepping": ([C.c_void_p, _DP, _DP, C.c_double, C.c_double], C.c_int),
+    "gpmood_setdt_time_stepping": ([C.c_void_p, _DP, _DP, C.c_double, C.c_double, C.POINTER(C.c_double)], C.c_int),
     "gpmood_set_state": ([C.c_void_p, _DP, C.c_double], C.c_int),
     "gpmood_get_state": ([C.c_void_p, _DP, _DP, C.POINTER(C.c_int)], C.c_int),
     "gpmood_get_orders": ([C.c_void_p, C.POINTER(C.c_byte)], C.c_int),
@@ -267,6 +268,15 @@ class Solver:
     def setdt_ptr(self, u_ptr: int, dtfinal: float) -> float:
         dt = C.c_double()
         self._check(self.lib.gpmood_setdt(self._h, C.cast(C.c_void_p(u_ptr), _DP), dtfinal, C.byref(dt)))
+        return dt.value
+
+    def setdt_time_stepping_ptr(self, uin_ptr: int, uout_ptr: int, t: float, dtfinal: float) -> float:
+        """Setdt + time_stepping in one call on host pointers (one upload, one
+        download); returns the dt taken."""
+        dt = C.c_double()
+        self._check(self.lib.gpmood_setdt_time_stepping(self._h, C.cast(C.c_void_p(uin_ptr), _DP),
+                                                        C.cast(C.c_void_p(uout_ptr), _DP), t, dtfinal,
+                                                        C.byref(dt)))
         return dt.value
 
     def time_stepping_dev(self, d_uin: int, d_uout: int, t: float, dt: float) -> None:

@@ -150,6 +150,13 @@ int  gpmood_setdt(gpmood_ctx* ctx, const double* u_host, double dtfinal, double*
 int  gpmood_time_stepping(gpmood_ctx* ctx, const double* uin_host, double* uout_host,
                           double t, double dt);
 
+/* Setdt(U) then time_stepping(U, Uout) (main.f90:151-155) in one call: U
+ * crosses to the GPU once and Uout once back, *dt_out receives the step
+ * taken.  Same results as gpmood_setdt + gpmood_time_stepping on the same
+ * arrays (same kernels on the same data). */
+int  gpmood_setdt_time_stepping(gpmood_ctx* ctx, const double* uin_host, double* uout_host,
+                                double t, double dtfinal, double* dt_out);
+
 /* ---- device-resident stepping ---- */
 
 /* Upload a state (Fortran layout) and the time; resets the step counter. */

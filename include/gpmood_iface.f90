@@ -4,6 +4,8 @@
 !     call Setdt(U)                    ->  ierr = gpmood_setdt(ctx, U, tmax - t, dt)
 !     call time_stepping(U, Ur)        ->  ierr = gpmood_time_stepping(ctx, U, Ur, t, dt)
 !     call Boundary_C(U)               ->  ierr = gpmood_boundary_c(ctx, U, t_rk)
+! or, for the two per-step calls together (one upload of U, one download):
+!     ierr = gpmood_setdt_time_stepping(ctx, U, Ur, t, tmax - t, dt)
 ! U and Ur keep their declaration real(8), dimension(4, lb:le, nb:ne)
 ! (gp-mood-code/global_variables.f90:26): that memory layout is the library's.
 ! The parameters module's knobs go into gpmood_params once, at start-up.
@@ -69,6 +71,16 @@ module gpmood_iface
          real(c_double), dimension(*), intent(in) :: uin
          real(c_double), dimension(*), intent(out) :: uout
          real(c_double), value :: t, dt
+      end function
+
+      integer(c_int) function gpmood_setdt_time_stepping(ctx, uin, uout, t, dtfinal, dt) &
+            bind(C, name="gpmood_setdt_time_stepping")
+         import :: c_int, c_ptr, c_double
+         type(c_ptr), value :: ctx
+         real(c_double), dimension(*), intent(in) :: uin
+         real(c_double), dimension(*), intent(out) :: uout
+         real(c_double), value :: t, dtfinal
+         real(c_double), intent(out) :: dt
       end function
 
       integer(c_int) function gpmood_set_state(ctx, u, t) bind(C, name="gpmood_set_state")

@@ -180,3 +180,23 @@ def test_mood_cap_is_an_error_and_the_context_survives(pkg, oracle):
         s.time_stepping(U, out, 0.0, dt)
         assert s.counters().max_passes_stage > 1
     assert nan_equal(out, ref)
+
+
+def test_one_call_step_equals_the_two_calls(pkg, oracle):
+    """gpmood_setdt_time_stepping = gpmood_setdt + gpmood_time_stepping, bit for bit."""
+    p = oracle.make_params(48, 40, bc=17, tmax=0.8)
+    U = oracle.initial_condition(p, "rp2d3")
+    kw = dict(lf=48, nf=40, bc_type=17, tmax=0.8, fp_mode=pkg.FP_EXACT)
+    with pkg.Solver(**kw) as a, pkg.Solver(**kw) as b:
+        Ua, Ub, ta, tb = U.copy(), U.copy(), 0.0, 0.0
+        for _ in range(4):
+            dta = a.Setdt(Ua, 0.8 - ta)
+            Ura = np.empty_like(Ua)
+            a.time_stepping(Ua, Ura, ta, dta)
+            Urb = np.empty_like(Ub)
+            dtb = b.setdt_time_stepping_ptr(Ub.ctypes.data, Urb.ctypes.data, tb, 0.8 - tb)
+            assert dtb == dta
+            assert nan_equal(Urb, Ura)
+            ta += dta
+            tb += dtb
+            Ua, Ub = Ura, Urb
