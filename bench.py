@@ -373,6 +373,8 @@ def run_final(args):
                      "mood_passes": tm.mood_passes,
                      "us_per_mood_pass": tm.mood_ms * 1e3 / tm.mood_passes if tm.mood_passes else None,
                      "final_state": {"sum_rho": float(U[4:-4, 4:-4, 0].sum()), "sum_E": float(U[4:-4, 4:-4, 3].sum())}}
+        # each variant on stderr as soon as it ends, so that a long run that is cut off still reports
+        print(json.dumps({"partial": name, "case": args.case, **out[name]}), file=sys.stderr, flush=True)
     if args.nn:
         out["nn_gated"]["speedup_vs_plain"] = out["plain"]["seconds"] / out["nn_gated"]["seconds"]
         out["rel_l1_final"] = _rel_l1(finals["nn_gated"], finals["plain"])

@@ -93,7 +93,8 @@ struct DevScalars {
     unsigned long long apriori_step;
 };
 
-enum { GPM_STATUS_NAN = 1, GPM_STATUS_MOODCAP = 2, GPM_STATUS_DT = 4, GPM_STATUS_BARRIER = 8 };
+enum { GPM_STATUS_NAN = 1, GPM_STATUS_MOODCAP = 2, GPM_STATUS_DT = 4, GPM_STATUS_BARRIER = 8,
+       GPM_STATUS_TENSOR = 16 };  // a tensor-core (tcgen05) wait timed out
 
 // Grid barrier state of the cooperative MOOD-loop kernel (zeroed device memory).
 struct GridBar {

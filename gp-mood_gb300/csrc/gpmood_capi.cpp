@@ -133,7 +133,8 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, int bc_stage)
             rc = nn_ref_orders(c->nnref, c->g, uin, c->dOrder, &c->dSc->apriori_step, nullptr, s);
             nnref = true;
         } else {  // gated cells start at mord-2 and are listed in tlist[1]
-            rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1], s);
+            rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1],
+                                nullptr, &c->dSc->status, s);
             fixup = true;
         }
         if (rc < 0) return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
@@ -307,6 +308,7 @@ int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
         cudaStreamSynchronize(s);
         return fail(c, GPMOOD_E_CUDA, "MOOD loop: grid barrier timed out");
     }
+    if (c->hSc->status & GPM_STATUS_TENSOR) return fail(c, GPMOOD_E_CUDA, "NN gate: tensor-core wait timed out");
     if (c->hSc->status & GPM_STATUS_MOODCAP) {
         const long long cap = c->p.max_mood_iters > 0 ? c->p.max_mood_iters : 2LL * c->p.lf * c->p.nf + 2;
         return fail(c, GPMOOD_E_MOOD_CAP, "MOOD loop did not converge in %lld passes", cap);
@@ -794,6 +796,23 @@ int gpmood_nn_ref_logits(gpmood_ctx* c, float* d_logits) {
     return 0;
 }
 
+int gpmood_nn_gate_logits(gpmood_ctx* c, float* d_logits) {
+    if (!c || !d_logits) return fail(c, GPMOOD_E_ARG, "NULL argument");
+    if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
+    if (c->p.nn_reference || !nn_gate_loaded(c->nn)) return fail(c, GPMOOD_E_STATE, "no gate parameters loaded");
+    CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, c->stream));
+    CU(cudaMemsetAsync(&c->dSc->apriori_step, 0, sizeof(unsigned long long), c->stream));
+    CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), c->stream));
+    if (nn_gate_orders(c->nn, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1], d_logits,
+                       &c->dSc->status, c->stream) < 0)
+        return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
+    int st = 0;
+    CU(cudaMemcpyAsync(&st, &c->dSc->status, sizeof st, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    if (st & GPM_STATUS_TENSOR) return fail(c, GPMOOD_E_CUDA, "NN gate: tensor-core wait timed out");
+    return 0;
+}
+
 int gpmood_set_nn_threshold(gpmood_ctx* c, float thr) {
     if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
     nn_gate_set_threshold(c->nn, thr);
@@ -811,13 +830,16 @@ int gpmood_nn_predict(gpmood_ctx* c, signed char* gated, long long* n_gated) {
     CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), c->stream));
     if ((ref ? nn_ref_orders(c->nnref, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, nullptr, c->stream)
              : nn_gate_orders(c->nn, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1],
-                              c->stream)) < 0)
+                              nullptr, &c->dSc->status, c->stream)) < 0)
         return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
     CU(cudaMemcpy2DAsync(gated, (size_t)c->p.lf, c->dOrder + (size_t)GPM_NGC * c->g.nx + GPM_NGC, (size_t)c->g.nx,
                          (size_t)c->p.lf, (size_t)c->p.nf, cudaMemcpyDeviceToHost, c->stream));
     unsigned long long cnt = 0;
+    int st = 0;
     CU(cudaMemcpyAsync(&cnt, &c->dSc->apriori_step, sizeof cnt, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaMemcpyAsync(&st, &c->dSc->status, sizeof st, cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
+    if (st & GPM_STATUS_TENSOR) return fail(c, GPMOOD_E_CUDA, "NN gate: tensor-core wait timed out");
     const size_t nint = (size_t)c->p.lf * c->p.nf;
     for (size_t i = 0; i < nint; i++) gated[i] = (ref ? gated[i] == 1 : gated[i] < c->p.mord) ? 1 : 0;
     if (n_gated) *n_gated = (long long)cnt;

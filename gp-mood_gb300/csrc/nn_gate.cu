@@ -168,26 +168,144 @@ __device__ __forceinline__ void warp_forward(const SmemFwd& s, int r0, float b2,
 }
 
 // ---------------------------------------------------------------------------
-// The gate: a persistent CTA loads the BF16 weights once, then walks tiles of
-// 128 interior cells: features, MLP, order update.  A tile whose cells all
-// have constant stencils (never gated) skips the MLP.
-__global__ void __launch_bounds__(THREADS) k_gate(GridGeom g, const double* __restrict__ u, const float* __restrict__ p,
-                                               float thr, int8_t* __restrict__ order,
-                                               unsigned long long* __restrict__ count, int* __restrict__ list,
-                                               int* __restrict__ list_count) {
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    SmemFwd& s = *reinterpret_cast<SmemFwd*>(smem_raw);
-    __shared__ int8_t cst[ROWS];
-    __shared__ float logit[ROWS];
-    load_weights(s, p);
+// The gate on the 5th-generation tensor cores (tcgen05).  A persistent CTA of
+// 4 warps walks tiles of 128 interior cells; thread r owns row r of a tile
+// (TMEM lane r).  Per tile:
+//   X[128 x 48]  (BF16 features, zero-padded from 36) -> shared memory
+//   D1 = X . W0^T      3 MMAs  M128 N64 K16 -> TMEM columns 0..63 (FP32)
+//   H  = BF16(ReLU(D1 + b0))                    -> shared memory (tcgen05.ld, per row)
+//   D2 = H . W1^T      4 MMAs                  -> TMEM columns 64..127
+//   logit = sum_j BF16(ReLU(D2 + b1))_j * BF16(w2)_j + b2   (per row, FP32)
+// Operands sit in shared memory in the K-major, no-swizzle canonical layout:
+// 8x8 BF16 core matrices of 128 contiguous bytes (row r of a core matrix at
+// 16 r), K-adjacent core matrices 128 B apart (the descriptor's leading byte
+// offset) and 8-row groups KC*128 B apart (stride byte offset).  One thread
+// issues the MMAs and commits them to an mbarrier; every wait is bounded and a
+// timeout sets GPM_STATUS_TENSOR, frees the TMEM and leaves the kernel.
+constexpr int TC_THREADS = 128;
+constexpr int TC_COLS = 128;         // TMEM columns held by a CTA (D1: 0..63, D2: 64..127)
+constexpr int TC_SMEM = 56 * 1024;   // dynamic shared memory requested: at most 4 CTAs (512 TMEM columns) per SM
+constexpr uint32_t TC_IDESC =        // kind::f16: D F32, A and B BF16, both K-major, N = 64, M = 128
+    (1u << 4) | (1u << 7) | (1u << 10) | ((64u >> 3) << 17) | ((128u >> 4) << 24);
+
+struct __align__(1024) SmemTc {
+    unsigned char w0[64 * 48 * 2];    // B of layer 0: 8 row groups x 6 k-chunks
+    unsigned char w1[64 * 64 * 2];    // B of layer 1: 8 x 8
+    unsigned char x[128 * 48 * 2];    // A of layer 0: 16 x 6
+    unsigned char h[128 * 64 * 2];    // A of layer 1: 16 x 8
+    float b0[64], b1[64], w2[64];
+    unsigned long long mbar;
+    uint32_t tmem;
+};
+static_assert(sizeof(SmemTc) <= TC_SMEM, "gate shared memory");
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Byte offset of element (r, k) of a K-major tile with kc 8-wide k-chunks.
+__device__ __forceinline__ uint32_t core_off(int r, int k, int kc) {
+    return (uint32_t)((r >> 3) * (kc * 128) + (k >> 3) * 128 + (r & 7) * 16 + (k & 7) * 2);
+}
+
+// Shared-memory matrix descriptor: start, leading and stride byte offsets
+// (16-byte units), descriptor version 1 (bits 46-48), no swizzle.
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+    return (uint64_t)((addr >> 4) & 0x3FFF) | ((uint64_t)((lbo >> 4) & 0x3FFF) << 16) |
+           ((uint64_t)((sbo >> 4) & 0x3FFF) << 32) | (1ull << 46);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t accumulate) {
+    asm volatile(
+        "{\n.reg .pred p;\nsetp.ne.b32 p, %4, 0;\n"
+        "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n}\n" ::"r"(d),
+        "l"(a), "l"(b), "r"(TC_IDESC), "r"(accumulate));
+}
+
+__device__ __forceinline__ void tc_commit(unsigned long long* bar) {
+    asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(smem_u32(bar))
+                 : "memory");
+}
+
+// Bounded wait for the mbarrier phase `parity` (~1 s at most).
+__device__ __forceinline__ bool tc_wait(unsigned long long* bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 20); it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+// 32 consecutive FP32 columns of this thread's TMEM lane.
+__device__ __forceinline__ void tc_ld32(uint32_t taddr, float* v) {
+    uint32_t r[32];
+    asm volatile(
+        "tcgen05.ld.sync.aligned.32x32b.x32.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15,"
+        "%16,%17,%18,%19,%20,%21,%22,%23,%24,%25,%26,%27,%28,%29,%30,%31}, [%32];\n"
+        "tcgen05.wait::ld.sync.aligned;\n"
+        : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]),
+          "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]),
+          "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]),
+          "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31])
+        : "r"(taddr)
+        : "memory");
+#pragma unroll
+    for (int j = 0; j < 32; j++) v[j] = __uint_as_float(r[j]);
+}
+
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;" ::: "memory"); }
+__device__ __forceinline__ void tc_before_sync() { asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory"); }
+__device__ __forceinline__ void tc_after_sync() { asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory"); }
+
+__global__ void __launch_bounds__(TC_THREADS) k_gate(GridGeom g, const double* __restrict__ u,
+                                                  const float* __restrict__ p, float thr, int8_t* __restrict__ order,
+                                                  unsigned long long* __restrict__ count, int* __restrict__ list,
+                                                  int* __restrict__ list_count, float* __restrict__ logits,
+                                                  int* __restrict__ status) {
+    extern __shared__ __align__(1024) unsigned char smem_raw[];
+    SmemTc& s = *reinterpret_cast<SmemTc*>(smem_raw);
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // weights, BF16, in the K-major core-matrix layout
+    for (int i = tid; i < 64 * 48; i += TC_THREADS) {
+        const int o = i / 48, k = i % 48;
+        *reinterpret_cast<__nv_bfloat16*>(s.w0 + core_off(o, k, 6)) =
+            __float2bfloat16_rn(k < 36 ? p[P_W0 + o * 36 + k] : 0.f);
+    }
+    for (int i = tid; i < 64 * 64; i += TC_THREADS)
+        *reinterpret_cast<__nv_bfloat16*>(s.w1 + core_off(i / 64, i % 64, 8)) = __float2bfloat16_rn(p[P_W1 + i]);
+    for (int i = tid; i < 64; i += TC_THREADS) {
+        s.b0[i] = p[P_B0 + i];
+        s.b1[i] = p[P_B1 + i];
+        s.w2[i] = bf16r(p[P_W2 + i]);
+    }
     const float b2 = p[P_B2];
+    if (warp == 0) {
+        asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&s.tmem)),
+                     "r"(TC_COLS));
+        asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;");
+    }
+    if (tid == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_u32(&s.mbar)));
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    fence_async_smem();
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    const uint32_t tmem = s.tmem;
+    const uint32_t lane_base = (uint32_t)(32 * warp) << 16;
+    const uint32_t sx = smem_u32(s.x), sh = smem_u32(s.h), sw0 = smem_u32(s.w0), sw1 = smem_u32(s.w1);
+    uint32_t phase = 0;
+    bool timed_out = false;
     const long long ncells = (long long)g.lf * g.nf;
-    const long long ntiles = (ncells + ROWS - 1) / ROWS;
-    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const long long ntiles = (ncells + TC_THREADS - 1) / TC_THREADS;
     for (long long tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
-        const long long row = tile * ROWS + threadIdx.x;
+        const long long row = tile * TC_THREADS + tid;
         bool c = true;
-        if (threadIdx.x < ROWS) {
+        {
             float x[36];
             if (row < ncells) {
                 const int l = 1 + (int)(row % g.lf), n = 1 + (int)(row / g.lf);
@@ -197,26 +315,90 @@ __global__ void __launch_bounds__(THREADS) k_gate(GridGeom g, const double* __re
                 for (int k = 0; k < 36; k++) x[k] = 0.f;
             }
 #pragma unroll
-            for (int k = 0; k < K0; k += 2)
-                *reinterpret_cast<uint32_t*>(&s.x[threadIdx.x][k]) =
-                    pack_bf16(k < 36 ? x[k] : 0.f, k + 1 < 36 ? x[k + 1] : 0.f);
-            cst[threadIdx.x] = c ? 1 : 0;
+            for (int kc = 0; kc < 6; kc++) {  // one 16-byte row of a core matrix per k-chunk
+                uint32_t w[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int k = 8 * kc + 2 * e;
+                    w[e] = pack_bf16(k < 36 ? x[k] : 0.f, k + 1 < 36 ? x[k + 1] : 0.f);
+                }
+                *reinterpret_cast<uint4*>(s.x + core_off(tid, 8 * kc, 6)) = make_uint4(w[0], w[1], w[2], w[3]);
+            }
         }
-        if (__syncthreads_and(c)) continue;  // every stencil constant: nothing to gate
-        WarpFwd f;
-        warp_forward(s, 16 * warp, b2, f);
-        if ((lane & 3) == 0) {
-            logit[16 * warp + (lane >> 2)] = f.logit_lo;
-            logit[16 * warp + (lane >> 2) + 8] = f.logit_hi;
+        fence_async_smem();
+        if (__syncthreads_and(c)) {  // every stencil constant: nothing to gate
+            if (logits && row < ncells) logits[row] = 0.f;
+            continue;
         }
+        // layer 0
+        if (tid == 0) {
+            tc_after_sync();
+#pragma unroll
+            for (int k = 0; k < 3; k++) tc_mma(tmem, tc_desc(sx + 256 * k, 128, 768), tc_desc(sw0 + 256 * k, 128, 768), k > 0);
+            tc_commit(&s.mbar);
+        }
+        bool ok = tc_wait(&s.mbar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            timed_out = true;
+            break;
+        }
+        tc_after_sync();
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            float d[32];
+            tc_ld32(tmem + lane_base + 32 * half, d);
+#pragma unroll
+            for (int kc = 0; kc < 4; kc++) {
+                uint32_t w[4];
+#pragma unroll
+                for (int e = 0; e < 4; e++) {
+                    const int j = 8 * kc + 2 * e, o = 32 * half + j;
+                    w[e] = pack_bf16(fmaxf(d[j] + s.b0[o], 0.f), fmaxf(d[j + 1] + s.b0[o + 1], 0.f));
+                }
+                *reinterpret_cast<uint4*>(s.h + core_off(tid, 32 * half + 8 * kc, 8)) = make_uint4(w[0], w[1], w[2], w[3]);
+            }
+        }
+        fence_async_smem();
+        tc_before_sync();
         __syncthreads();
+        // layer 1
+        if (tid == 0) {
+            tc_after_sync();
+#pragma unroll
+            for (int k = 0; k < 4; k++)
+                tc_mma(tmem + 64, tc_desc(sh + 256 * k, 128, 1024), tc_desc(sw1 + 256 * k, 128, 1024), k > 0);
+            tc_commit(&s.mbar);
+        }
+        ok = tc_wait(&s.mbar, phase);
+        phase ^= 1;
+        if (__syncthreads_or(!ok)) {
+            timed_out = true;
+            break;
+        }
+        tc_after_sync();
+        float z = 0.f;
+#pragma unroll
+        for (int half = 0; half < 2; half++) {
+            float d[32];
+            tc_ld32(tmem + lane_base + 64 + 32 * half, d);
+#pragma unroll
+            for (int j = 0; j < 32; j++) {
+                const int o = 32 * half + j;
+                z += bf16r(fmaxf(d[j] + s.b1[o], 0.f)) * s.w2[o];
+            }
+        }
+        z += b2;
         bool fire = false;
         int cidx = 0;
-        if (threadIdx.x < ROWS && row < ncells && !cst[threadIdx.x] && logit[threadIdx.x] > thr) {
-            const int l = 1 + (int)(row % g.lf), n = 1 + (int)(row / g.lf);
-            cidx = (n + 3) * g.nx + (l + 3);
-            order[cidx] = (int8_t)(g.mord - 2);
-            fire = true;
+        if (row < ncells) {
+            if (logits) logits[row] = c ? 0.f : z;
+            if (!c && z > thr) {
+                const int l = 1 + (int)(row % g.lf), n = 1 + (int)(row / g.lf);
+                cidx = (n + 3) * g.nx + (l + 3);
+                order[cidx] = (int8_t)(g.mord - 2);
+                fire = true;
+            }
         }
         const unsigned m = __ballot_sync(0xffffffffu, fire);
         if (m) {  // warp-aggregated append to the gated-cell list
@@ -228,8 +410,14 @@ __global__ void __launch_bounds__(THREADS) k_gate(GridGeom g, const double* __re
             base = __shfl_sync(0xffffffffu, base, 0);
             if (fire) list[base + __popc(m & ((1u << lane) - 1))] = cidx;
         }
-        __syncthreads();  // s.x, cst and logit are rewritten by the next tile
+        tc_before_sync();
+        __syncthreads();  // X, H and the TMEM columns are rewritten by the next tile
     }
+    if (timed_out && tid == 0) atomicOr(status, GPM_STATUS_TENSOR);
+    tc_before_sync();
+    __syncthreads();
+    tc_after_sync();
+    if (warp == 0) asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC_COLS));
 }
 
 __global__ void k_features(GridGeom g, const double* __restrict__ u, float* __restrict__ x, int8_t* __restrict__ cst) {
@@ -525,21 +713,22 @@ void nn_gate_set_threshold(NnGate* n, float thr) { n->thr = thr; }
 bool nn_gate_loaded(const NnGate* n) { return n && n->loaded; }
 
 int nn_gate_orders(NnGate* n, const GridGeom& g, const double* uin, int8_t* order, unsigned long long* count,
-                   int* list, int* list_count, cudaStream_t s) {
+                   int* list, int* list_count, float* logits, int* status, cudaStream_t s) {
     if (!n->loaded || g.mord < 3) return 0;
     const long long cells = (long long)g.lf * g.nf;
-    const long long tiles = (cells + ROWS - 1) / ROWS;
-    const size_t sm = sizeof(SmemFwd);
+    const long long tiles = (cells + TC_THREADS - 1) / TC_THREADS;
     static int nsm = 0;
     if (!nsm) {
         int dev = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         if (nsm <= 0) nsm = 1;
-        cudaFuncSetAttribute(k_gate, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
+        cudaFuncSetAttribute(k_gate, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
     }
-    const int blocks = (int)(tiles < 4LL * nsm ? tiles : 4LL * nsm);  // persistent: up to 4 CTAs per SM
-    k_gate<<<blocks, THREADS, sm, s>>>(g, uin, n->params, n->thr, order, count, list, list_count);
+    // persistent: 4 CTAs per SM, each holding 128 of the SM's 512 TMEM columns
+    const int blocks = (int)(tiles < 4LL * nsm ? tiles : 4LL * nsm);
+    k_gate<<<blocks, TC_THREADS, TC_SMEM, s>>>(g, uin, n->params, n->thr, order, count, list, list_count, logits,
+                                               status);
     return cudaGetLastError() == cudaSuccess ? 1 : -1;
 }
 

@@ -6,7 +6,7 @@
 // each variable divided by its max-abs over the stencil, feature index
 // v*9 + j.  MLP 36 -> 64 -> 64 -> 1 with ReLU hidden layers and a sigmoid
 // output; BF16 operands with FP32 accumulation on the tensor cores
-// (mma.sync m16n8k16).  A positive prediction (logit > threshold) starts the
+// (inference: tcgen05.mma with TMEM accumulators; training: mma.sync m16n8k16).  A positive prediction (logit > threshold) starts the
 // cell at reduced order (mord - 2) before the first MOOD pass; the
 // a-posteriori DETECTION stays on unchanged.  Cells whose stencil is constant
 // in every variable are never gated, as in the reference's format_input
@@ -35,9 +35,12 @@ void nn_gate_set_threshold(NnGate* n, float logit_threshold);
 bool nn_gate_loaded(const NnGate* n);
 // Overwrite order[] of gated interior cells with mord-2; adds the number of
 // gated cells to *count and appends their padded indices to list (running
-// length *list_count).  Returns the number of kernels launched, or -1.
+// length *list_count); logits[lf*nf] (may be NULL) receives every interior
+// cell's logit (0 for constant stencils).  The MLP runs on the tcgen05 tensor
+// cores; a tensor-core wait that times out sets GPM_STATUS_TENSOR in *status.
+// Returns the number of kernels launched, or -1.
 int nn_gate_orders(NnGate* n, const GridGeom& g, const double* uin, int8_t* order, unsigned long long* count,
-                   int* list, int* list_count, cudaStream_t s);
+                   int* list, int* list_count, float* logits, int* status, cudaStream_t s);
 
 // Features (FP32, [n][36]) and constant-stencil flags of every interior cell
 // (x fastest), for callers that evaluate or train the network themselves.

@@ -82,6 +82,7 @@ SIGNATURES = {
     "gpmood_set_nn": ([C.c_void_p, C.POINTER(C.c_float), C.c_int], C.c_int),
     "gpmood_set_nn_threshold": ([C.c_void_p, C.c_float], C.c_int),
     "gpmood_nn_ref_logits": ([C.c_void_p, C.c_void_p], C.c_int),
+    "gpmood_nn_gate_logits": ([C.c_void_p, C.c_void_p], C.c_int),
     "gpmood_nn_predict": ([C.c_void_p, C.POINTER(C.c_byte), C.POINTER(C.c_longlong)], C.c_int),
     "gpmood_get_stage_orders": ([C.c_void_p, C.c_int, C.POINTER(C.c_byte)], C.c_int),
     "gpmood_nn_features": ([C.c_void_p, C.c_void_p, C.c_void_p], C.c_int),
@@ -329,6 +330,10 @@ class Solver:
     def nn_ref_logits(self, d_logits: int) -> None:
         """r(1), r(2) of the reference's network for every interior cell (device array)."""
         self._check(self.lib.gpmood_nn_ref_logits(self._h, C.c_void_p(d_logits)))
+
+    def nn_gate_logits(self, d_logits: int) -> None:
+        """The gate's logit of every interior cell (device float array of lf*nf)."""
+        self._check(self.lib.gpmood_nn_gate_logits(self._h, C.c_void_p(d_logits)))
 
     def set_nn_threshold(self, logit_threshold: float) -> None:
         self._check(self.lib.gpmood_set_nn_threshold(self._h, float(logit_threshold)))

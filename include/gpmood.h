@@ -256,6 +256,9 @@ int  gpmood_set_nn(gpmood_ctx* ctx, const float* params, int n);
  * the device-resident state into d_logits[2*lf*nf] (0, 0 for constant
  * stencils); nn_reference = 1 only. */
 int  gpmood_nn_ref_logits(gpmood_ctx* ctx, float* d_logits);
+/* The gate's logit of every interior cell of the device-resident state into
+ * d_logits[lf*nf] (0 for constant stencils; nn_reference = 0). */
+int  gpmood_nn_gate_logits(gpmood_ctx* ctx, float* d_logits);
 /* The gate fires when the logit exceeds this value (default 0, i.e. p > 0.5). */
 int  gpmood_set_nn_threshold(gpmood_ctx* ctx, float logit_threshold);
 /* Gate decision on the device-resident state: gated[lf*nf] = 1 where the cell

@@ -50,8 +50,9 @@ def features(U: np.ndarray, lf: int, nf: int):
                  axis=-1)  # [nf, lf, 4, 9]
     mx, mn = q.max(axis=-1), q.min(axis=-1)
     am = np.abs(q).max(axis=-1)
-    scale = np.where(am > 0, np.float32(1.0) / np.where(am > 0, am, 1), 0).astype(np.float32)
-    x = (q * scale[..., None]).reshape(nf * lf, 36)
+    with np.errstate(over="ignore", invalid="ignore"):  # subnormal max-abs: 1/am = inf, as in FP32 on the GPU
+        scale = np.where(am > 0, np.float32(1.0) / np.where(am > 0, am, 1), 0).astype(np.float32)
+        x = (q * scale[..., None]).reshape(nf * lf, 36)
     cst = np.all((mx - mn) < np.float32(1e-10), axis=-1).reshape(-1)
     return x.astype(np.float32), cst
 

@@ -109,6 +109,30 @@ def test_gate_decision_matches_oracle(pkg, oracle, nno):
     assert ref.sum() > 0 and (~ref & ~cst).sum() > 0
 
 
+@pytest.mark.parametrize("ic,bc,tmax,steps", [("rp2d3", 17, 0.8, 3), ("sedov", 20, 0.05, 6)])
+def test_tensor_core_gate_logits_match_oracle(pkg, oracle, nno, ic, bc, tmax, steps):
+    """The tcgen05 gate (TMEM accumulators) against the BF16-emulating numpy
+    forward: same roundings of inputs, weights and hidden activations, FP32
+    sums in another order (tolerance as the training forward's).  300x200 is
+    not a multiple of the 128-cell tile."""
+    lf, nf = 300, 200
+    U = _state(oracle, ic, lf, nf, bc, tmax, steps)
+    p = _params(13, scale=2.0)
+    with pkg.Solver(lf=lf, nf=nf, bc_type=bc, method=pkg.NN_GP_MOOD) as s:
+        s.set_state(U, 0.0)
+        s.set_nn(p)
+        z = torch.full((lf * nf,), float("nan"), dtype=torch.float32, device="cuda")
+        s.nn_gate_logits(z.data_ptr())
+        zg = z.cpu().numpy()
+        mask, cnt = s.nn_predict()
+    x, cst = nno.features(U, lf, nf)
+    zr, _ = nno.forward(p, x, emulate_bf16=True)
+    assert np.all(zg[cst] == 0)
+    np.testing.assert_allclose(zg[~cst], zr[~cst], rtol=2e-3, atol=2e-3)
+    got = mask.ravel().astype(bool)
+    assert np.array_equal(got, (zg > 0) & ~cst) and cnt == int(got.sum())
+
+
 def test_harvest_labels_are_the_stage1_mood_decisions(pkg, oracle, nno):
     lf = nf = 64
     U = _state(oracle, "sedov", lf, nf, 20, 0.05, 4)
