@@ -416,6 +416,7 @@ int gpmood_batch_advance(gpmood_batch* b, int nsteps) {
         b->dt_pending = true;
         b->steps++;
         b->detected += b->hntrb[4];
+        if (b->hntrb[6]) b->status |= GPM_STATUS_NAN;  // a NaN or inadmissible state left at order 1
         if (b->hbar->err) return bfail(b, GPMOOD_E_CUDA, "batched MOOD loop: grid barrier timed out");
         if (b->hntrb[3]) {
             b->status |= GPM_STATUS_MOODCAP;

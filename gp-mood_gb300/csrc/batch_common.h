@@ -39,7 +39,8 @@ struct BatchArgs {
     int8_t* order;
     unsigned* stamp;
     int2* tlist[2];
-    int* ntrb;            // [0..1] list counts, [2] pass epoch, [3] cap flag, [4] detected, [5] passes
+    int* ntrb;            // [0..1] list counts, [2] pass epoch, [3] cap flag, [4] detected, [5] passes,
+                          // [6] NaN or inadmissible state left in an order-1 cell (sticky)
     const int4* ftiles;
     int nftiles;
     const int4* etiles;   // edge items of the two-direction cell tiles

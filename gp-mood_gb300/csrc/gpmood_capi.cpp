@@ -242,6 +242,7 @@ int run_rk4(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
 int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
     cudaStream_t s = c->stream;
     CU(cudaMemsetAsync(&c->dSc->detected_step, 0, 2 * sizeof(unsigned long long), s));
+    CU(cudaMemsetAsync(&c->dSc->status, 0, sizeof(int), s));  // this step's flags (counters keep them all)
     int rc = 0;
     if (c->p.integrator == GPMOOD_SSP_RK3) {  // SSP_RK3_, mod_SSP_RK3.f90:12-39
         rc = run_stage(c, u, c->dU1, 0, 0);

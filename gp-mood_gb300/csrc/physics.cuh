@@ -436,6 +436,18 @@ __device__ __forceinline__ bool shock_detector(const Cell& c, const Cell& L, con
 }
 #endif
 
+// An order-1 cell is never checked again (mod_subroutine_MOOD.f90:41), so a
+// NaN or non-positive density or pressure in it survives the stage; callers
+// report it (GPM_STATUS_NAN) without changing the result.
+__device__ __forceinline__ bool inadmissible(const Cell& uo) {
+    if (le_zero_or_nan(uo.r)) return true;
+#if GPM_EXACT
+    return le_zero_or_nan(pressure(uo));
+#else
+    return le_zero_or_nan(pressure_ir(uo, gpm_fast_rcp(uo.r)));
+#endif
+}
+
 // DETECTION checks for one interior cell (mod_subroutine_MOOD.f90:41-131).
 // uin points at Uin(1, l, n) of a padded array of row pitch 4*nx doubles.
 // The DMP bounds test runs before the shock detector: both are side-effect

@@ -529,6 +529,7 @@ __global__ void __launch_bounds__(256) k_update_detect(StageArgs a, const __grid
     if (g.method == 2 || g.method == 203) {
         const int o = a.uniform_order ? g.mord : (int)a.order[c];
         if (o > 1) trb = mood_troubled(uo, a.uin + 4 * c, g.nx, g, w.d2x, w.d2y);
+        else if (inadmissible(uo)) atomicOr(&a.sc->status, GPM_STATUS_NAN);
     }
     if (trb) cascade_order(&a.order[c]);
     list_append(trb, a.tlist[cur], &a.sc->ntrb[cur], (int)c);
@@ -716,6 +717,7 @@ __global__ void __launch_bounds__(256) k_mood_cells(StageArgs a, const __grid_co
                 const Cell uo = cell_update(g, a.uin, a.fx, a.fy, c, qx, qy);
                 st_cell(a.uout + 4 * c, uo);
                 if (a.order[c] > 1) trb = mood_troubled(uo, a.uin + 4 * c, g.nx, g, w.d2x, w.d2y);
+                else if (inadmissible(uo)) atomicOr(&a.sc->status, GPM_STATUS_NAN);
                 cval = (int)c;
             }
         }
@@ -832,6 +834,7 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
                     const Cell uo = cell_update(g, a.uin, a.fx, a.fy, c, qx, qy);
                     st_cell(a.uout + 4 * c, uo);
                     if (a.order[c] > 1) trb = mood_troubled(uo, a.uin + 4 * c, g.nx, g, w.d2x, w.d2y);
+                    else if (inadmissible(uo)) atomicOr(&a.sc->status, GPM_STATUS_NAN);
                     cval = (int)c;
                 }
             }
@@ -1281,6 +1284,8 @@ __global__ void __launch_bounds__(256) kb_update(BatchArgs a) {
             st_cell(a.uout + 4 * (P.off + (long long)c), uo);
             if (a.method == 2 && g.mord > 1)
                 trb = mood_troubled(uo, ub + 4 * c, g.nx, g, a.wtab[P.wc].d2x, a.wtab[P.wc].d2y);
+            else if (a.method == 2 && inadmissible(uo))
+                atomicOr(&a.ntrb[6], 1);
             cl = (int)c;
         }
         if (trb) cascade_order(a.order + P.off + cl);
@@ -1357,6 +1362,8 @@ __global__ void __launch_bounds__(256) kb_mood_cells(BatchArgs a, int cur) {
                 st_cell(a.uout + 4 * (P.off + (long long)c), uo);
                 if (a.order[P.off + (long long)c] > 1)
                     trb = mood_troubled(uo, ub + 4 * c, g.nx, g, a.wtab[P.wc].d2x, a.wtab[P.wc].d2y);
+                else if (inadmissible(uo))
+                    atomicOr(&a.ntrb[6], 1);
                 val = make_int2(e.x, (int)c);
             }
         }
@@ -1433,6 +1440,8 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) kb_mood_loop(BatchArgs a, Gri
                     st_cell(a.uout + 4 * (P.off + (long long)c), uo);
                     if (a.order[P.off + (long long)c] > 1)
                         trb = mood_troubled(uo, ub + 4 * c, g.nx, g, a.wtab[P.wc].d2x, a.wtab[P.wc].d2y);
+                    else if (inadmissible(uo))
+                        atomicOr(&a.ntrb[6], 1);
                     val = make_int2(e.x, (int)c);
                 }
             }

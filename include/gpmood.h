@@ -98,8 +98,11 @@ typedef struct gpmood_counters {
     long long mood_passes_last_step;/* passes summed over the 3 stages */
     long long max_passes_stage;     /* worst stage since create */
     long long steps;                /* steps taken through this context */
-    long long status_flags;         /* bit 0: NaN/inadmissible state left in an
-                                       order-1 cell; bit 1: MOOD cap hit; bit 2: bad dt */
+    long long status_flags;         /* OR of every step's flags.  bit 0: NaN/inadmissible
+                                       state left in an order-1 cell (reported, the step
+                                       still succeeds, as in the reference); bit 1: MOOD cap
+                                       hit; bit 2: bad dt; bit 3: grid-barrier timeout;
+                                       bit 4: tensor-core wait timeout */
     long long kernel_launches;      /* kernels launched through this context */
 } gpmood_counters;
 

@@ -200,3 +200,34 @@ def test_one_call_step_equals_the_two_calls(pkg, oracle):
             ta += dta
             tb += dtb
             Ua, Ub = Ura, Urb
+
+
+@pytest.mark.parametrize("bad", ["negative_pressure", "nan_density"])
+def test_inadmissible_state_is_caught_and_reported(pkg, oracle, bad):
+    """An inadmissible cell planted in the initial array (SURVEY-style fault
+    injection on the host): MOOD lowers the cells around it to first order,
+    the bad values stay in order-1 cells, the step equals the oracle bit for
+    bit, and status bit 0 reports the state left in an order-1 cell without
+    failing the call."""
+    ic, lf, nf, kn = CASES["rp2d3"]
+    p = _oracle_params(oracle, lf, nf, kn)
+    U = oracle.initial_condition(p, ic)
+    dt = oracle.setdt(p, U, p.tmax)
+    j, i = 4 + 20, 4 + 30  # interior cell (l, n) = (31, 21)
+    if bad == "negative_pressure":
+        U[j, i, 3] = 0.5 * (U[j, i, 1] ** 2 + U[j, i, 2] ** 2) / U[j, i, 0] - 1.0
+    else:
+        U[j, i, 0] = np.nan
+    ref = np.empty_like(U)
+    oracle.Stepper(p).time_stepping(U.copy(), ref, 0.0, dt)
+    with _solver(pkg, lf, nf, pkg.FP_EXACT, kn) as s:
+        out = np.empty_like(U)
+        s.time_stepping(U, out, 0.0, dt)
+        flags = s.counters().status_flags
+        orders = s.orders()
+    assert nan_equal(out, ref)
+    assert flags & 1
+    assert orders[j - 4, i - 4] == 1
+    interior = out[4:-4, 4:-4]
+    bad_cells = ~np.isfinite(interior).all(axis=-1)
+    assert bad_cells.any() and bad_cells.sum() < 50  # local, not spread over the grid
