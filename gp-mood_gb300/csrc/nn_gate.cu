@@ -1,8 +1,9 @@
-// nn_gate.cu -- a-priori MLP gate: features, BF16 tensor-core inference,
-// training sample harvest, and BF16 tensor-core forward/backward + Adam.
+// nn_gate.cu -- a-priori MLP gate: features, BF16 tensor-core inference
+// (tcgen05, k_gate below), training sample harvest, and BF16 tensor-core
+// forward/backward + Adam.
 //
-// Every matrix product runs as mma.sync.m16n8k16 with BF16 operands and FP32
-// accumulation.  A CTA handles 128 rows (cells or samples), 16 per warp.
+// The training products run as mma.sync.m16n8k16 with BF16 operands and FP32
+// accumulation; a CTA handles 128 rows (samples), 16 per warp.
 // Fragment layouts (PTX ISA, m16n8k16 .bf16): with g = lane/4, t = lane%4,
 //   A (16x16, row): a0 = A[g][2t..2t+1], a1 = A[g+8][2t..], a2 = A[g][2t+8..], a3 = A[g+8][2t+8..]
 //   B (16x8, col) : b0 = B[2t..2t+1][g], b1 = B[2t+8..2t+9][g]

@@ -6,8 +6,9 @@
 // each variable divided by its max-abs over the stencil, feature index
 // v*9 + j.  MLP 36 -> 64 -> 64 -> 1 with ReLU hidden layers and a sigmoid
 // output; BF16 operands with FP32 accumulation on the tensor cores
-// (inference: tcgen05.mma with TMEM accumulators; training: mma.sync m16n8k16).  A positive prediction (logit > threshold) starts the
-// cell at reduced order (mord - 2) before the first MOOD pass; the
+// (inference: tcgen05.mma with TMEM accumulators; training: mma.sync
+// m16n8k16).  A positive prediction (logit > threshold) starts the cell at
+// reduced order (mord - 2) before the first MOOD pass; the
 // a-posteriori DETECTION stays on unchanged.  Cells whose stencil is constant
 // in every variable are never gated, as in the reference's format_input
 // (gp-mood-code/mod_append_NN_dataset.f90:96-114).  The gate's role is that of
