@@ -50,7 +50,7 @@ def parse():
     ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
     ap.add_argument("--n", type=int, default=N_DEFAULT)
     ap.add_argument("--fp-mode", choices=("fast", "exact"), default="fast")
-    ap.add_argument("--e2e-steps", type=int, default=5)
+    ap.add_argument("--e2e-steps", type=int, default=10)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--nn", type=int, default=1, help="also time the NN-gated variant (0: skip)")
     ap.add_argument("--batch-problems", type=int, default=1024)
