@@ -74,6 +74,7 @@ struct GridGeom {
     int dmp, u2, u2_tol;
     int num_flux;        // 100 HLLC, 101 LLF, 102 HLL, 103 unsplit
     int mood_solo;       // device MOOD loop: lists of at most this many cells run in one CTA
+    int cc_col;          // NN_GP_MOOD_CC: the column l whose order-3 states are blended (-1: none)
 };
 
 // Default of GridGeom::mood_solo; the environment variable GPMOOD_MOOD_SOLO
@@ -115,6 +116,8 @@ struct StageArgs {
     DevScalars* sc;
     int uniform_order;     // 1: every cell starts at mord (plain GP-MOOD)
     int stage;             // 0, 1, 2 -> t_rk = t, t+dt, t+dt/2
+    const float* ccw;      // NN_GP_MOOD_CC: (v1, v2) of column g.cc_col per row n (2 floats per row
+                           // 0..nf+1); NULL: no blend (every other method, and warm-up steps)
 };
 
 // Host-side launchers implemented once per floating-point variant

@@ -42,6 +42,8 @@ struct gpmood_ctx {
     gpmood_counters ctr;
     NnGate* nn;                   // a-priori gate and training kernels
     NnRef* nnref;                 // the reference's own network (nn_reference = 1)
+    bool cc;                      // method NN_GP_MOOD_CC (kept as NN_GP_MOOD + nn_reference + cc)
+    float* dCcw;                  // NN_GP_MOOD_CC: values_NN(L, n, :) per row, 2*(nf+2) floats
     int8_t* dStageOrd;            // CellGPO at the end of each RK stage (GPM_MAXST x ncell)
     int nstages;                  // Forward_Euler calls per step: FE 1, SSP-RK2 2, SSP-RK3 3, SSP-RK4 5
     double* dRk4[5];              // SSP-RK4 work arrays U3, U4, FU3, FU4, Fl (U1, U2 are dU1, dU2)
@@ -111,6 +113,7 @@ StageArgs stage_args(gpmood_ctx* c, const double* uin, double* uout, int stage, 
     a.sc = c->dSc;
     a.uniform_order = uniform ? 1 : 0;
     a.stage = stage;
+    a.ccw = nullptr;
     return a;
 }
 
@@ -122,27 +125,36 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, int bc_stage)
     cudaStream_t s = c->stream;
     const KernelTable& kt = *c->kt;
     cudaEvent_t* ev = c->ev[stage];
-    c->kt->bc(c->g, uin, c->dSc, bc_stage, s);  // Boundary_C(Uin), :64
-    c->ctr.kernel_launches += 2;
     bool uniform = true, fixup = false, nnref = false;
     CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, s));  // CellGPO = mord, :48
     CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), s));
-    if (c->p.method == GPMOOD_NN_GP_MOOD && c->niter + 1 > c->p.nsteps_with_no_nn) {  // :51-56
-        int rc;
-        if (c->p.nn_reference) {  // the reference's network sets every CellGPO to 1 or 3
-            rc = nn_ref_orders(c->nnref, c->g, uin, c->dOrder, &c->dSc->apriori_step, nullptr, s);
-            nnref = true;
-        } else {  // gated cells start at mord-2 and are listed in tlist[1]
-            rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1],
-                                nullptr, &c->dSc->status, s);
-            fixup = true;
-        }
+    const bool nn_on = c->p.method == GPMOOD_NN_GP_MOOD && c->niter + 1 > c->p.nsteps_with_no_nn;  // :51
+    if (nn_on && c->p.nn_reference) {
+        // the reference's network sets every CellGPO to 1 or 3; it reads Uin
+        // before Boundary_C, as mod_FE.f90:51-56 come before :64
+        const int rc = nn_ref_orders(c->nnref, c->g, uin, c->dOrder, &c->dSc->apriori_step, nullptr,
+                                     c->cc ? c->dCcw : nullptr, s);
         if (rc < 0) return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
         c->ctr.kernel_launches += rc;
+        nnref = true;
+        uniform = false;
+    }
+    c->kt->bc(c->g, uin, c->dSc, bc_stage, s);  // Boundary_C(Uin), :64
+    c->ctr.kernel_launches += 2;
+    if (nn_on && !c->p.nn_reference) {  // gated cells start at mord-2 and are listed in tlist[1]
+        const int rc = nn_gate_orders(c->nn, c->g, uin, c->dOrder, &c->dSc->apriori_step, c->dList[1],
+                                      &c->dSc->ntrb[1], nullptr, &c->dSc->status, s);
+        if (rc < 0) return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));
+        c->ctr.kernel_launches += rc;
+        fixup = true;
         uniform = false;
     }
     StageArgs a = stage_args(c, uin, uout, stage, uniform);
     if (nnref) a.g.dmp = 0;  // NN_DETECTION: NaN and positivity only (mod_subroutine_NN_MOOD.f90:22-35)
+    if (nnref && c->cc) {    // NN_GP_MOOD_CC_ reconstruction (mod_Reconstruction.f90:26-31)
+        a.ccw = c->dCcw;
+        a.g.cc_col = nn_ref_inputs(c->p.mord);
+    }
     if (c->timing) cudaEventRecord(ev[0], s);
     // First pass over every face at mord; the faces of gated cells are then
     // recomputed at min(CellGPO) of their two cells, which gives every stored
@@ -332,8 +344,12 @@ int validate(const gpmood_params* p, char* why, size_t n) {
     if (p->integrator != GPMOOD_FE && p->integrator != GPMOOD_SSP_RK2 && p->integrator != GPMOOD_SSP_RK3 &&
         p->integrator != GPMOOD_SSP_RK4) {
         snprintf(why, n, "integrator %d unsupported (FE=8, SSP_RK2=9, SSP_RK3=10, SSP_RK4=12)", p->integrator); return -1; }
-    if (p->method != GPMOOD_GP_MOOD && p->method != GPMOOD_GP_SE && p->method != GPMOOD_NN_GP_MOOD) {
-        snprintf(why, n, "method %d unsupported (GP_MOOD=2, GP_SE=202, NN_GP_MOOD=203)", p->method); return -1; }
+    if (p->method != GPMOOD_GP_MOOD && p->method != GPMOOD_GP_SE && p->method != GPMOOD_NN_GP_MOOD &&
+        p->method != GPMOOD_NN_GP_MOOD_CC) {
+        snprintf(why, n, "method %d unsupported (GP_MOOD=2, GP_SE=202, NN_GP_MOOD=203, NN_GP_MOOD_CC=204)", p->method);
+        return -1; }
+    if (p->method == GPMOOD_NN_GP_MOOD_CC && p->mord != 3) {  // mod_NN_GP_MOOD_CC.f90:73 stops above order 3
+        snprintf(why, n, "NN_GP_MOOD_CC needs Mord 3"); return -1; }
     if (p->num_flux < GPMOOD_HLLC || p->num_flux > GPMOOD_UNSPLIT) {
         snprintf(why, n, "numFlux %d unsupported (HLLC=100, LLF=101, HLL=102, unsplit=103)", p->num_flux); return -1; }
     if (!(p->mord == 1 || p->mord == 3 || p->mord == 5)) { snprintf(why, n, "Mord %d unsupported (1, 3, 5)", p->mord); return -1; }
@@ -360,6 +376,7 @@ void free_all(gpmood_ctx* c) {
     if (c->hCount) cudaFreeHost(c->hCount);
     if (c->nn) nn_gate_destroy(c->nn);
     if (c->nnref) nn_ref_destroy(c->nnref);
+    if (c->dCcw) cudaFree(c->dCcw);
     for (int st = 0; st < GPM_MAXST; st++)
         for (int i = 0; i < 4; i++)
             if (c->ev[st][i]) cudaEventDestroy(c->ev[st][i]);
@@ -404,6 +421,11 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     c = new (std::nothrow) gpmood_ctx();
     if (!c) return fail(nullptr, GPMOOD_E_ARG, "out of host memory");
     c->p = *p;
+    c->cc = p->method == GPMOOD_NN_GP_MOOD_CC;
+    if (c->cc) {  // the reference's network with its convex-combination reconstruction
+        c->p.method = GPMOOD_NN_GP_MOOD;
+        c->p.nn_reference = 1;
+    }
     c->g.lf = p->lf;
     c->g.nf = p->nf;
     c->g.nx = p->lf + 2 * GPM_NGC;
@@ -414,9 +436,10 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     c->g.bc_type = p->bc_type;
     c->g.ngp = p->ngp;
     c->g.mord = p->mord;
-    c->g.method = p->method;
+    c->g.method = c->p.method;
     c->g.num_flux = p->num_flux;
     c->g.mood_solo = gpm_mood_solo_default();
+    c->g.cc_col = -1;
     c->nstages = p->integrator == GPMOOD_FE ? 1 : p->integrator == GPMOOD_SSP_RK2 ? 2 : p->integrator == GPMOOD_SSP_RK4 ? 5 : 3;
     c->g.dmp = p->dmp;
     c->g.u2 = p->u2;
@@ -503,7 +526,8 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     }
     c->nn = nn_gate_create(c->g);
     c->nnref = nn_ref_create();
-    if (!c->nn || !c->nnref) {
+    if (c->cc && cudaMalloc(&c->dCcw, sizeof(float) * 2 * (size_t)(p->nf + 2)) != cudaSuccess) c->dCcw = nullptr;
+    if (!c->nn || !c->nnref || (c->cc && !c->dCcw)) {
         fail(c, GPMOOD_E_CUDA, "NN gate allocation failed");
         free_all(c);
         delete c;
@@ -791,7 +815,8 @@ int gpmood_nn_ref_logits(gpmood_ctx* c, float* d_logits) {
     if (!c->have_state) return fail(c, GPMOOD_E_STATE, "no device-resident state (call gpmood_set_state)");
     if (!c->p.nn_reference || !nn_ref_loaded(c->nnref)) return fail(c, GPMOOD_E_STATE, "no reference network loaded");
     CU(cudaMemsetAsync(&c->dSc->apriori_step, 0, sizeof(unsigned long long), c->stream));
-    if (nn_ref_orders(c->nnref, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, d_logits, c->stream) < 0)
+    if (nn_ref_orders(c->nnref, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, d_logits, c->cc ? c->dCcw : nullptr,
+                      c->stream) < 0)
         return fail(c, GPMOOD_E_CUDA, "reference network: %s", cudaGetErrorString(cudaGetLastError()));
     CU(cudaStreamSynchronize(c->stream));
     return 0;
@@ -829,7 +854,8 @@ int gpmood_nn_predict(gpmood_ctx* c, signed char* gated, long long* n_gated) {
     CU(cudaMemsetAsync(c->dOrder, c->p.mord, c->ncell, c->stream));
     CU(cudaMemsetAsync(&c->dSc->apriori_step, 0, sizeof(unsigned long long), c->stream));
     CU(cudaMemsetAsync(c->dSc->ntrb, 0, sizeof(c->dSc->ntrb), c->stream));
-    if ((ref ? nn_ref_orders(c->nnref, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, nullptr, c->stream)
+    if ((ref ? nn_ref_orders(c->nnref, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, nullptr,
+                             c->cc ? c->dCcw : nullptr, c->stream)
              : nn_gate_orders(c->nn, c->g, c->dU, c->dOrder, &c->dSc->apriori_step, c->dList[1], &c->dSc->ntrb[1],
                               nullptr, &c->dSc->status, c->stream)) < 0)
         return fail(c, GPMOOD_E_CUDA, "NN gate: %s", cudaGetErrorString(cudaGetLastError()));

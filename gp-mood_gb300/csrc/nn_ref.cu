@@ -11,7 +11,12 @@
 // x1 = sigmoid(W1 x0 + b1), r = W2 x1 + b2 in FP32 (sigmoid 1/(1+exp(-x)) in
 // FP32, constants.f90:65); r(1) > r(2) sets CellGPO = 1 and counts an
 // a-priori detection, else CellGPO = 3.  Sums run in index order without FMA
-// contraction.
+// contraction.  With the convex-combination method (NN_GP_MOOD_CC) the
+// outputs pass through softmax first (forward, mod_NN.f90:181) and the
+// decision compares the softmaxed pair; every row n also leaves the pair of
+// its last cell (l = lf; (0, 1) for a constant stencil) in ccw[2n..2n+1]:
+// the reference stores each cell's pair in values_NN(L, n, :), L the input
+// count (mod_NN.f90:41,44), so the last write of the row stays.
 #include <cuda_runtime.h>
 
 #include <new>
@@ -34,7 +39,7 @@ __device__ __forceinline__ float sigmoid_ref(float x) {
 __global__ void __launch_bounds__(THREADS) k_nn_ref(GridGeom g, const double* __restrict__ u,
                                                     const float* __restrict__ p, int len, int npts,
                                                     int8_t* __restrict__ order, unsigned long long* __restrict__ count,
-                                                    float* __restrict__ logits) {
+                                                    float* __restrict__ logits, float* __restrict__ ccw) {
     extern __shared__ float w[];
     const int L = 4 * npts;
     const int nparam = len * L + len + len * len + len + 2 * len + 2;
@@ -72,7 +77,14 @@ __global__ void __launch_bounds__(THREADS) k_nn_ref(GridGeom g, const double* __
         const size_t ci = (size_t)(n + 3) * g.nx + (size_t)(l + 3);
         if (cst) {
             order[ci] = 3;
-            if (logits) logits[2 * cell] = logits[2 * cell + 1] = 0.0f;
+            if (logits) {
+                logits[2 * cell] = 0.0f;
+                logits[2 * cell + 1] = ccw ? 1.0f : 0.0f;
+            }
+            if (ccw && l == g.lf) {
+                ccw[2 * n] = 0.0f;
+                ccw[2 * n + 1] = 1.0f;
+            }
             continue;
         }
         float h0[128], r0 = b2[0], r1 = b2[1];
@@ -91,6 +103,15 @@ __global__ void __launch_bounds__(THREADS) k_nn_ref(GridGeom g, const double* __
         }
         r0 = __fadd_rn(s0, r0);
         r1 = __fadd_rn(s1, r1);
+        if (ccw) {  // softmax, mod_NN.f90:132-145
+            const float e0 = expf(r0), e1 = expf(r1), d = __fadd_rn(e0, e1);
+            r0 = __fdiv_rn(e0, d);
+            r1 = __fdiv_rn(e1, d);
+            if (l == g.lf) {
+                ccw[2 * n] = r0;
+                ccw[2 * n + 1] = r1;
+            }
+        }
         if (logits) {
             logits[2 * cell] = r0;
             logits[2 * cell + 1] = r1;
@@ -144,7 +165,7 @@ int nn_ref_set(NnRef* r, const float* params, int n, int mord, cudaStream_t s) {
 bool nn_ref_loaded(const NnRef* r) { return r && r->params && r->len > 0; }
 
 int nn_ref_orders(NnRef* r, const GridGeom& g, const double* uin, int8_t* order, unsigned long long* count,
-                  float* logits, cudaStream_t s) {
+                  float* logits, float* ccw, cudaStream_t s) {
     if (!nn_ref_loaded(r)) return -1;
     const int L = 4 * r->npts;
     const size_t sm = sizeof(float) * ((size_t)r->len * L + r->len * r->len + 4 * r->len + 2);
@@ -159,6 +180,6 @@ int nn_ref_orders(NnRef* r, const GridGeom& g, const double* uin, int8_t* order,
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     const long long want = (cells + THREADS - 1) / THREADS;
     const int blocks = (int)(want < 4LL * sms ? want : 4LL * sms);
-    k_nn_ref<<<blocks, THREADS, sm, s>>>(g, uin, r->params, r->len, r->npts, order, count, logits);
+    k_nn_ref<<<blocks, THREADS, sm, s>>>(g, uin, r->params, r->len, r->npts, order, count, logits, ccw);
     return cudaGetLastError() == cudaSuccess ? 1 : -1;
 }

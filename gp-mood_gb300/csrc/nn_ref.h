@@ -21,6 +21,9 @@ int nn_ref_set(NnRef* r, const float* params, int n, int mord, cudaStream_t s);
 bool nn_ref_loaded(const NnRef* r);
 // CellGPO of every interior cell (1 or 3) from the network on uin; adds the
 // cells set to 1 to *count; logits[2*cell] = r(1), r(2) if logits != NULL.
-// Returns the number of kernels launched, or -1.
+// ccw != NULL selects NN_GP_MOOD_CC: r passes through softmax (logits hold
+// values_NN, (0, 1) for constant stencils) and ccw[2n..2n+1], n = 1..nf,
+// receives the pair of the row's last cell.  Returns the number of kernels
+// launched, or -1.
 int nn_ref_orders(NnRef* r, const GridGeom& g, const double* uin, int8_t* order, unsigned long long* count,
-                  float* logits, cudaStream_t s);
+                  float* logits, float* ccw, cudaStream_t s);

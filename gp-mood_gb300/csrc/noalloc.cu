@@ -95,6 +95,7 @@ int stage_noalloc(const KernelTable& kt, const GridGeom& g, const GpWeights& w, 
     a.sc = s.sc;
     a.uniform_order = 1;
     a.stage = stage;
+    a.ccw = nullptr;
     kt.flux_all(a, w, st);
     kt.update_detect(a, w, 0, st);
     NCU(cudaGetLastError());
@@ -167,6 +168,7 @@ extern "C" int gpmood_time_stepping_noalloc(const gpmood_params* p, double* d_ui
     g.dmp = p->dmp;
     g.u2 = p->u2;
     g.u2_tol = p->u2_tol;
+    g.cc_col = -1;
     GpWeights w;
     double inv_err[3];
     if (gpm_gp_presim(p->ell_o_dx, p->lx, p->ly, p->lf, p->nf, p->mord, p->ngp, &w, inv_err))

@@ -150,24 +150,63 @@ __device__ __forceinline__ void recon_face(const GpWeights& w, int o, int face, 
     gp_recon<NP, NGP>(&w.zt[o][face][0][0], q, u);
 }
 
+// NN_GP_MOOD_CC_ (mod_NN_GP_MOOD_CC.f90:63-70): with the reference network
+// on, a face state of cell (l, n) at order 1 is the cell value itself and at
+// order 3 the blend v1*U(l,n) + v2*Uh with (v1, v2) = values_NN(l, n) taken
+// to double.  values_NN is (0, 1) except in column g.cc_col of rows 1..nf:
+// the reference's network loop writes its outputs to values_NN(L, n, :)
+// (mod_NN.f90:41,44; Fortran reads `l` there as the input count L), so the
+// row's last cell leaves its softmax there.  A (0, 1) blend is applied like
+// any other, as the reference does.
+__device__ __forceinline__ void cc_weights(const GridGeom& g, const float* ccw, int l, int n, double* v1,
+                                           double* v2) {
+    *v1 = 0.0;
+    *v2 = 1.0;
+    if (l == g.cc_col && n >= 1 && n <= g.nf) {
+        *v1 = (double)ccw[2 * n];
+        *v2 = (double)ccw[2 * n + 1];
+    }
+}
+
+template <int NP>
+__device__ __forceinline__ void cc_blend(double v1, double v2, const Cell& c, double* u) {
+    const double cv[4] = {c.r, c.mx, c.my, c.e};
+#pragma unroll
+    for (int k = 0; k < 4; k++) u[k] = NP == 1 ? cv[k] : v1 * cv[k] + v2 * u[k];
+}
+
+// ccw != NULL (NN_GP_MOOD_CC): (l, n) is the low cell of the face.
 template <int DIR, int NP, int NGP>
 __device__ __forceinline__ void face_from_tile(const GpWeights& w, int o, const Cell (*tile)[HX], int tx, int ty,
-                                               double* F, int nflux) {
+                                               double* F, int nflux, const float* ccw = nullptr,
+                                               const GridGeom* g = nullptr, int l = 0, int n = 0) {
     constexpr int FL = DIR == 0 ? 2 : 1;  // iR (x) / iT (y) face of the low cell
     constexpr int FH = DIR == 0 ? 0 : 3;  // iL (x) / iB (y) face of the high cell
+    constexpr int hx = DIR == 0 ? 1 : 0, hy = DIR == 0 ? 0 : 1;
     double uL[NGP][4], uR[NGP][4];
     {
         Cell q[NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) q[m] = tile[ty + st_oy(m)][tx + st_ox(m)];
         recon_face<DIR, NP, NGP>(w, o, FL, q, uL);
+        if (ccw) {
+            double v1, v2;
+            cc_weights(*g, ccw, l, n, &v1, &v2);
+#pragma unroll
+            for (int j = 0; j < NGP; j++) cc_blend<NP>(v1, v2, q[0], uL[j]);
+        }
     }
     {
-        constexpr int hx = DIR == 0 ? 1 : 0, hy = DIR == 0 ? 0 : 1;
         Cell q[NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) q[m] = tile[ty + hy + st_oy(m)][tx + hx + st_ox(m)];
         recon_face<DIR, NP, NGP>(w, o, FH, q, uR);
+        if (ccw) {
+            double v1, v2;
+            cc_weights(*g, ccw, l + hx, n + hy, &v1, &v2);
+#pragma unroll
+            for (int j = 0; j < NGP; j++) cc_blend<NP>(v1, v2, q[0], uR[j]);
+        }
     }
     quad_flux<DIR, NGP>(uL, uR, w.gw, F, nflux);
 }
@@ -195,8 +234,8 @@ __global__ void __launch_bounds__(TX * TY) k_flux_tile(StageArgs a, const __grid
         const size_t c0 = cidx(g, l, n), c1 = DIR == 0 ? c0 + 1 : c0 + g.nx;
         const int o = min((int)a.order[c0], (int)a.order[c1]);
         if (o >= 5) face_from_tile<DIR, 13, NGP>(w, 2, tile, tx, ty, F, g.num_flux);
-        else if (o >= 3) face_from_tile<DIR, 5, NGP>(w, 1, tile, tx, ty, F, g.num_flux);
-        else face_from_tile<DIR, 1, NGP>(w, 0, tile, tx, ty, F, g.num_flux);
+        else if (o >= 3) face_from_tile<DIR, 5, NGP>(w, 1, tile, tx, ty, F, g.num_flux, a.ccw, &g, l, n);
+        else face_from_tile<DIR, 1, NGP>(w, 0, tile, tx, ty, F, g.num_flux, a.ccw, &g, l, n);
     }
     double* out = (DIR == 0 ? a.fx : a.fy) + 4 * cidx(g, l, n);
     st_cell(out, Cell{F[0], F[1], F[2], F[3]});
@@ -602,22 +641,34 @@ struct FaceGp {
 template <int DIR, int NP>
 __device__ __forceinline__ void face_gp_states(const GridGeom& g, const GpWeights& w, int o,
                                                const double* __restrict__ uin, size_t c0, int gp, double* uL,
-                                               double* uR) {
+                                               double* uR, const float* ccw) {
     constexpr int FL = DIR == 0 ? 2 : 1;
     constexpr int FH = DIR == 0 ? 0 : 3;
+    constexpr int hx = DIR == 0 ? 1 : 0, hy = DIR == 0 ? 0 : 1;
     const ptrdiff_t row = g.nx;
     const size_t c1 = DIR == 0 ? c0 + 1 : c0 + g.nx;
+    const int l0 = (int)(c0 % (size_t)g.nx) - 3, n0 = (int)(c0 / (size_t)g.nx) - 3;  // low cell (l, n)
     {
         Cell q[NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) q[m] = ld_cell(uin + 4 * (c0 + st_ox(m) + row * st_oy(m)));
         gp_recon_at<NP>(&w.zt[o][FL][gp][0], q, uL);
+        if (ccw) {
+            double v1, v2;
+            cc_weights(g, ccw, l0, n0, &v1, &v2);
+            cc_blend<NP>(v1, v2, q[0], uL);
+        }
     }
     {
         Cell q[NP];
 #pragma unroll
         for (int m = 0; m < NP; m++) q[m] = ld_cell(uin + 4 * (c1 + st_ox(m) + row * st_oy(m)));
         gp_recon_at<NP>(&w.zt[o][FH][gp][0], q, uR);
+        if (ccw) {
+            double v1, v2;
+            cc_weights(g, ccw, l0 + hx, n0 + hy, &v1, &v2);
+            cc_blend<NP>(v1, v2, q[0], uR);
+        }
     }
 }
 
@@ -632,9 +683,9 @@ __device__ __forceinline__ void face_gp_any(const StageArgs& a, const GpWeights&
     const size_t c1 = DIR == 0 ? c0 + 1 : c0 + g.nx;
     const int o = min((int)a.order[c0], (int)a.order[c1]);
     double uL[4], uR[4];
-    if (o >= 5) face_gp_states<DIR, 13>(g, w, 2, a.uin, c0, gp, uL, uR);
-    else if (o >= 3) face_gp_states<DIR, 5>(g, w, 1, a.uin, c0, gp, uL, uR);
-    else face_gp_states<DIR, 1>(g, w, 0, a.uin, c0, gp, uL, uR);
+    if (o >= 5) face_gp_states<DIR, 13>(g, w, 2, a.uin, c0, gp, uL, uR, nullptr);
+    else if (o >= 3) face_gp_states<DIR, 5>(g, w, 1, a.uin, c0, gp, uL, uR, a.ccw);
+    else face_gp_states<DIR, 1>(g, w, 0, a.uin, c0, gp, uL, uR, a.ccw);
     riemann<DIR>(g.num_flux, uL, uR, f.F);
     f.out = (DIR == 0 ? a.fx : a.fy) + 4 * c0;
     f.gw = w.gw;
@@ -1071,6 +1122,7 @@ __device__ __forceinline__ GridGeom bgeom(const BatchArgs& a, const BProb& p) {
     g.bc_type = a.bc_type; g.ngp = a.ngp; g.mord = a.mord; g.method = a.method;
     g.dmp = a.dmp; g.u2 = a.u2; g.u2_tol = a.u2_tol; g.num_flux = a.num_flux;
     g.mood_solo = a.mood_solo;
+    g.cc_col = -1;
     return g;
 }
 
@@ -1307,6 +1359,7 @@ __device__ __forceinline__ void kb_face_gp(const BatchArgs& a, int cur, int nt, 
     const int2 e = a.tlist[cur][face_item(i, nt, &dir, &side)];
     const BProb P = a.prob[e.x];
     StageArgs sa;
+    sa.ccw = nullptr;
     sa.g = bgeom(a, P);
     sa.uin = a.uin + 4 * P.off;
     sa.fx = a.fx + 4 * P.off;

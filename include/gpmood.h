@@ -39,6 +39,8 @@ extern "C" {
 #define GPMOOD_GP_MOOD     2     /* method: GP-MOOD */
 #define GPMOOD_GP_SE       202   /* method: unlimited GP (MOOD off) */
 #define GPMOOD_NN_GP_MOOD  203   /* method: GP-MOOD with the MLP a-priori gate */
+#define GPMOOD_NN_GP_MOOD_CC 204 /* method: the reference's network with its convex-combination
+                                    reconstruction (mod_NN_GP_MOOD_CC.f90); Mord 3 */
 #define GPMOOD_FE          8     /* integrator: Forward_Euler */
 #define GPMOOD_SSP_RK2     9
 #define GPMOOD_SSP_RK3     10
@@ -72,7 +74,7 @@ typedef struct gpmood_params {
     double lx, ly;        /* domain [0,Lx]x[0,Ly] (Lx_16, Ly_16)       :43-44 */
     double tmax;          /* final time                                :41 */
     int integrator;       /* GPMOOD_FE, _SSP_RK2, _SSP_RK3, _SSP_RK4   :9  */
-    int method;           /* GPMOOD_GP_MOOD, GPMOOD_GP_SE, GPMOOD_NN_GP_MOOD */
+    int method;           /* GPMOOD_GP_MOOD, GPMOOD_GP_SE, GPMOOD_NN_GP_MOOD, GPMOOD_NN_GP_MOOD_CC */
     int mord;             /* maximal order 1, 3 or 5                   :15 */
     int ngp;              /* Gauss points per face, 1..5               :16 */
     int dmp, u2, u2_tol;  /* MOOD checks (logical -> 0/1)              :18-20 */

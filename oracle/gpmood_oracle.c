@@ -598,7 +598,28 @@ struct orc_ctx {
     unsigned char *detcell, *detfx, *detfy, *decrease;
     double *u1, *u2;
     double *rk4[5];  /* U3, U4, FU3, FU4, Fl of SSP_RK4_ (U1, U2 are u1, u2), on first use */
+    int cc_col;      /* NN_GP_MOOD_CC_ blend column (the input count L), or -1 */
+    float *cc_w;     /* values_NN(cc_col, n, 1:2) for n = 0..nf+1; NULL: no blend */
 };
+
+/* NN_GP_MOOD_CC_ (mod_NN_GP_MOOD_CC.f90:11-85): with w != NULL every face
+ * state of order 1 is the cell value and every one of order 3 is
+ * real(v1,8)*Uin + real(v2,8)*Uh, (v1, v2) = values_NN(l, n, :): (0, 1) except
+ * column col of rows 1..nf, where w[2n], w[2n+1] hold the pair the
+ * reference's network loop leaves there (mod_NN.f90:41,44 write
+ * values_NN(L, n, :); Fortran reads `l` as the input count L). */
+void orc_set_cc(orc_ctx* c, int col, const float* w)
+{
+    free(c->cc_w);
+    c->cc_w = NULL;
+    c->cc_col = -1;
+    if (!w) return;
+    const size_t n = 2 * (size_t)(c->p.nf + 2);
+    c->cc_w = (float*)malloc(n * sizeof(float));
+    if (!c->cc_w) return;
+    memcpy(c->cc_w, w, n * sizeof(float));
+    c->cc_col = col;
+}
 
 orc_ctx* orc_create(const orc_params* p)
 {
@@ -634,6 +655,7 @@ void orc_destroy(orc_ctx* c)
     free(c->uh); free(c->lfx); free(c->lfy); free(c->cellgpo); free(c->detcell);
     free(c->detfx); free(c->detfy); free(c->decrease); free(c->u1); free(c->u2);
     for (int i = 0; i < 5; i++) free(c->rk4[i]);
+    free(c->cc_w);
     free(c);
 }
 
@@ -679,6 +701,18 @@ static void recons(orc_ctx* c, const double* Uin)
                         for (int m = 0; m < np; m++) s = s + c->gp.zt[o][i][j][m] * q[m][k];
                         UH(c, me, i, j)[k] = s;
                     }
+                if (c->cc_w) { /* mod_NN_GP_MOOD_CC.f90:63-70 */
+                    double v1 = 0.0, v2 = 1.0;
+                    if (l == c->cc_col && n >= 1 && n <= G.nf) {
+                        v1 = (double)c->cc_w[2 * n];
+                        v2 = (double)c->cc_w[2 * n + 1];
+                    }
+                    for (int j = 0; j < ngp; j++)
+                        for (int k = 0; k < 4; k++) {
+                            double* u = &UH(c, me, i, j)[k];
+                            *u = ord == 1 ? q[0][k] : v1 * q[0][k] + v2 * *u;
+                        }
+                }
             }
         }
 }

@@ -86,6 +86,9 @@ int orc_time_stepping(orc_ctx* c, double* Uin, double* Uout, double t, double dt
                       signed char* const* stage_orders, long long* counters);
 
 /* One Forward_Euler stage (mod_FE.f90:20-190); exposed for unit tests. */
+/* NN_GP_MOOD_CC_ reconstruction: blend column col with the row pairs
+ * w[2n..2n+1], n = 0..nf+1 (copied); w = NULL switches it off. */
+void orc_set_cc(orc_ctx* c, int col, const float* w);
 int orc_forward_euler(orc_ctx* c, double* Uin, double* Uout, double dt, double t_rk,
                       const signed char* init_order, signed char* final_order,
                       long long* counters);

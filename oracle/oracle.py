@@ -76,6 +76,7 @@ def lib() -> C.CDLL:
         L.orc_create.argtypes = [P(OrcParams)]
         L.orc_create.restype = C.c_void_p
         L.orc_destroy.argtypes = [C.c_void_p]
+        L.orc_set_cc.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
         L.orc_time_stepping.argtypes = [C.c_void_p, dp, dp, C.c_double, C.c_double, C.c_void_p, C.c_void_p,
                                         P(C.c_longlong)]
         L.orc_shock_detector.argtypes = [P(OrcParams), dp, C.c_int, C.c_int]
@@ -143,6 +144,14 @@ class Stepper:
 
     def __del__(self):
         self.close()
+
+    def set_cc(self, col: int, w=None):
+        """NN_GP_MOOD_CC_ blend of column `col` with row pairs w[nf+2, 2] (None: off)."""
+        if w is None:
+            lib().orc_set_cc(self._h, -1, None)
+            return
+        a = np.ascontiguousarray(w, dtype=np.float32).reshape(self.p.nf + 2, 2)
+        lib().orc_set_cc(self._h, int(col), a.ctypes.data)
 
     def time_stepping(self, Uin: np.ndarray, Uout: np.ndarray, t: float, dt: float,
                       init_orders=None, want_orders: bool = False):

@@ -124,3 +124,66 @@ def test_reference_network_runs_equal_the_oracle(pkg, oracle, fire):
     assert tg == t
     I = (slice(4, -4), slice(4, -4))
     assert nan_equal(Ug[I], U[I]), np.nanmax(np.abs(Ug[I] - U[I]))
+
+
+def _constant_net(L, length, b2):
+    """A network whose outputs are b2 on every cell (zero weights)."""
+    p = np.zeros(length * L + length + length * length + length + 2 * length + 2, np.float32)
+    p[-2:] = b2
+    return p
+
+
+@pytest.mark.parametrize("fire", [False, True])
+def test_convex_combination_method_equals_the_oracle(pkg, oracle, fire):
+    """NN_GP_MOOD_CC (mod_NN_GP_MOOD_CC.f90): softmaxed outputs decide the
+    orders; order-3 states of column L = 52 (the reference's values_NN(l, ...)
+    with l read as L) are blended v1*U + v2*Uh with the row's last-cell pair,
+    order-1 states are the cell values.  Exact mode, bit for bit against the
+    oracle's blend with the pair the GPU's network produced."""
+    n, nsteps = 64, 4
+    U0 = _wavy(n)
+    net = _constant_net(52, 5, [0.5, -0.5] if fire else [-0.5, 0.5])
+    kw = dict(lf=n, nf=n, bc_type=18, tmax=0.8, mord=3, ngp=2, method=pkg.NN_GP_MOOD_CC, nsteps_with_no_nn=0,
+              fp_mode=pkg.FP_EXACT)
+    p = oracle.make_params(n, n, bc=18, tmax=0.8, mord=3, ngp=2, dmp=0)
+    U = U0.copy()
+    oracle.boundary(p, U)
+    Ug0 = U.copy()
+    with pkg.Solver(**kw) as s:
+        s.set_nn(net)
+        s.set_state(Ug0, 0.0)
+        d = torch.empty(2 * n * n, dtype=torch.float32, device="cuda")
+        s.nn_ref_logits(d.data_ptr())
+        v = d.cpu().numpy().reshape(n, n, 2)
+        assert np.allclose(v.sum(axis=-1), 1.0, atol=1e-6)  # softmax pairs
+        assert (v[..., 0] > v[..., 1]).all() == fire
+        assert s.advance(nsteps) == nsteps
+        Ug, tg, _ = s.get_state()
+        c = s.counters()
+    assert c.a_priori_last_step == (3 * n * n if fire else 0)
+    w = np.zeros((n + 2, 2), np.float32)
+    w[:, 1] = 1.0
+    w[1:n + 1] = v[:, n - 1]  # the pair of each row's last cell (l = lf)
+    st = oracle.Stepper(p)
+    st.set_cc(52, w)
+    ones = [np.ones((n, n), np.int8)] * 3
+    t = 0.0
+    for _ in range(nsteps):
+        dt = oracle.setdt(p, U, p.tmax - t)
+        Ur = np.empty_like(U)
+        st.time_stepping(U, Ur, t, dt, init_orders=ones if fire else None)
+        t += dt
+        U = Ur
+    assert tg == t
+    I = (slice(4, -4), slice(4, -4))
+    assert nan_equal(Ug[I], U[I]), np.nanmax(np.abs(Ug[I] - U[I]))
+    if not fire:  # the blend acted: the run differs from the same oracle run without it
+        st2 = oracle.Stepper(p)
+        U2, t2 = Ug0.copy(), 0.0
+        for _ in range(nsteps):
+            dt = oracle.setdt(p, U2, p.tmax - t2)
+            Ur = np.empty_like(U2)
+            st2.time_stepping(U2, Ur, t2, dt)
+            t2 += dt
+            U2 = Ur
+        assert not np.array_equal(U2[I], U[I])

@@ -120,3 +120,33 @@ def test_variants_conserve_mass_and_symmetry(oracle, integ, nflux):
     U, t, k, _ = run(oracle, p, "rp2d3", 4)
     r = U[I + (0,)]
     assert np.abs(r - r.T).sum() / r.size < 1e-12  # plot/plotter_hdf5.py:43, as above
+
+
+def test_convex_combination_blend_with_unit_weights_is_plain(oracle):
+    """The oracle's NN_GP_MOOD_CC_ blend with values_NN = (0, 1) everywhere
+    reproduces plain GP-MOOD at Mord 3 bit for bit; a non-trivial pair in one
+    column changes the run."""
+    n = 48
+    p = oracle.make_params(n, n, bc=17, tmax=0.8, mord=3, ngp=2)
+    U0 = oracle.initial_condition(p, "rp2d3")
+    w = np.zeros((n + 2, 2), np.float32)
+    w[:, 1] = 1.0
+
+    def run(wts):
+        st = oracle.Stepper(p)
+        if wts is not None:
+            st.set_cc(40, wts)
+        U, t = U0.copy(), 0.0
+        for _ in range(3):
+            dt = oracle.setdt(p, U, p.tmax - t)
+            Ur = np.empty_like(U)
+            st.time_stepping(U, Ur, t, dt)
+            t += dt
+            U = Ur
+        return U
+
+    plain, unit = run(None), run(w)
+    assert np.array_equal(plain, unit)
+    w2 = w.copy()
+    w2[1:n + 1] = [0.25, 0.75]
+    assert not np.array_equal(plain, run(w2))
