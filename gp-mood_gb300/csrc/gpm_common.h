@@ -92,6 +92,7 @@ struct DevScalars {
     unsigned stamp_epoch;             // first unused pass stamp of the device MOOD loop
     unsigned long long detected_step; // count_detected_cell of the current step
     unsigned long long apriori_step;
+    double bcd[4][4];                 // Dirichlet BC (19): the right ghost columns' states, from the host
 };
 
 enum { GPM_STATUS_NAN = 1, GPM_STATUS_MOODCAP = 2, GPM_STATUS_DT = 4, GPM_STATUS_BARRIER = 8,

@@ -356,7 +356,9 @@ int validate(const gpmood_params* p, char* why, size_t n) {
     if (p->ngp < 1 || p->ngp > 5) { snprintf(why, n, "ngp %d out of 1..5", p->ngp); return -1; }
     if (p->lf < 4 || p->nf < 4 || p->lf > 65536 || p->nf > 65536) { snprintf(why, n, "grid %dx%d out of range", p->lf, p->nf); return -1; }
     if (p->bc_type != GPMOOD_NEUMANN && p->bc_type != GPMOOD_PERIODIC && p->bc_type != GPMOOD_REFLECTIVE &&
-        p->bc_type != GPMOOD_DMR) { snprintf(why, n, "BC_type %d unsupported", p->bc_type); return -1; }
+        p->bc_type != GPMOOD_DMR && p->bc_type != GPMOOD_DIRICHLET && p->bc_type != GPMOOD_MACH800 &&
+        p->bc_type != GPMOOD_DOUBLE_MACH800 && p->bc_type != GPMOOD_RMI && p->bc_type != GPMOOD_RT &&
+        p->bc_type != GPMOOD_KH) { snprintf(why, n, "BC_type %d unsupported", p->bc_type); return -1; }
     if (!(p->cfl > 0) || !(p->lx > 0) || !(p->ly > 0) || !(p->ell_o_dx > 0)) { snprintf(why, n, "CFL, Lx, Ly, ell_o_dx must be > 0"); return -1; }
     if (p->fp_mode != GPMOOD_FP_EXACT && p->fp_mode != GPMOOD_FP_FAST) { snprintf(why, n, "fp_mode %d unknown", p->fp_mode); return -1; }
     if (p->max_mood_iters < 0) { snprintf(why, n, "max_mood_iters must be >= 0 (0: no cap but termination)"); return -1; }
@@ -507,6 +509,16 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     memset(c->hSc, 0, sizeof(DevScalars));
     c->hSc->tmax = p->tmax;
     c->hSc->cfl = p->cfl;
+    if (p->bc_type == GPMOOD_DIRICHLET)  // BC.f90:68: sin() on the host, as the CPU restatement does
+        for (int j = 0; j < GPM_NGC; j++) {
+            const int l = p->lf + 1 + j;
+            const double x = l * c->g.dx - c->g.dx / 2, r = 1. + 0.2 * sin(5 * (x - 4.5));
+            double* q = c->hSc->bcd[j];
+            q[0] = r;
+            q[1] = r * 0.;
+            q[2] = r * 0.;
+            q[3] = ((1. / (1.4 - 1.)) + 0.5 * r * (0. * 0. + 0. * 0.));  // p2c(r, 0, 0, 1), gamma = 1.4
+        }
     c->hSc->dtmin_bits = 0x46293e5939a08ceaULL;  // bits of 1.0e30
     // Initialise on the context's own stream: it is non-blocking, so work on the
     // legacy default stream would not be ordered before its first kernels.

@@ -86,6 +86,30 @@ __global__ void k_bc_x(GridGeom g, double* __restrict__ u, const DevScalars* __r
         dst[0] = src[0]; dst[1] = -src[1]; dst[2] = src[2]; dst[3] = src[3];
     } else if (g.bc_type == 35) {  // DMR: exact pre/post-shock states
         f_dmr(l * g.dx - g.dx / 2, n * g.dy - g.dy / 2, dst);
+    } else if (g.bc_type == 19) {  // Dirichlet: the right states come from the host (sin), BC.f90:61-75
+        if (right) {
+            for (int v = 0; v < 4; v++) dst[v] = sc->bcd[j][v];
+        } else {
+            p2c(3.857143, 2.629369, 0., 10.33333, dst);
+        }
+    } else if (g.bc_type == 201 || g.bc_type == 301) {  // Mach800 jets: outflow in x, BC.f90:137-152
+        const double* src = u + 4 * cidx(g, right ? g.lf : 1, n);
+        for (int v = 0; v < 4; v++) dst[v] = src[v];
+    } else if (g.bc_type == 401) {  // RMI: inflow left, outflow right, BC.f90:243-256
+        if (right) {
+            const double* src = u + 4 * cidx(g, g.lf, n);
+            for (int v = 0; v < 4; v++) dst[v] = src[v];
+        } else {
+            p2c(2.666666666666667, 2. * sqrt(1.4), 0., 4.5, dst);
+        }
+    } else if (g.bc_type == 402) {  // RT: reflective in x, BC.f90:344-362
+        const int ls = right ? g.lf - j : 1 + j;
+        const double* src = u + 4 * cidx(g, ls, n);
+        dst[0] = src[0]; dst[1] = -src[1]; dst[2] = src[2]; dst[3] = src[3];
+    } else if (g.bc_type == 403) {  // KH: periodic in x, BC.f90:394-400
+        const int ls = right ? 1 + j : g.lf - j;
+        const double* src = u + 4 * cidx(g, ls, n);
+        for (int v = 0; v < 4; v++) dst[v] = src[v];
     }
 }
 
@@ -122,6 +146,26 @@ __global__ void k_bc_y(GridGeom g, double* __restrict__ u, const DevScalars* __r
         } else {
             p2c(8., 7.1447096, -4.125, 116.5, dst);
         }
+    } else if (g.bc_type == 19 || g.bc_type == 403) {  // Neumann in y (BC.f90:77-87, :402-413)
+        const double* src = u + 4 * cidx(g, l, top ? g.nf : 1);
+        for (int v = 0; v < 4; v++) dst[v] = src[v];
+    } else if (g.bc_type == 201 || g.bc_type == 301) {  // outflow, then the jets (BC.f90:154-178, :199-236)
+        const double* src = u + 4 * cidx(g, l, top ? g.nf : 1);
+        for (int v = 0; v < 4; v++) dst[v] = src[v];
+        if (fabs((l * g.dx - g.dx / 2) - 0.75) <= 0.05) {
+            if (!top) p2c(1.4, 0.0, 800.0, 1.0, dst);
+            else if (g.bc_type == 301) p2c(1.4, 0.0, -800.0, 1.0, dst);
+        }
+    } else if (g.bc_type == 401) {  // RMI: reflective in y, BC.f90:258-280
+        const int ns = top ? g.nf - j : 1 + j;
+        const double* src = u + 4 * cidx(g, l, ns);
+        dst[0] = src[0]; dst[1] = src[1]; dst[2] = -src[2]; dst[3] = src[3];
+    } else if (g.bc_type == 402) {  // RT: hydrostatic ghosts, g = real(0.1, 4), BC.f90:364-389
+        const double* q = u + 4 * cidx(g, l, top ? g.nf - j : 1 + j);
+        const double grav = (double)0.1f;
+        const double pr = (GPM_GAMMA - 1.) * (q[3] - (0.5 * (q[1] * q[1] + q[2] * q[2]) / q[0]));
+        const double dp = 2 * j * g.dy * grav * q[0];
+        p2c(q[0], q[1] / q[0], -(q[2] / q[0]), top ? pr - dp : pr + dp, dst);
     }
 }
 

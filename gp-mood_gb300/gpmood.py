@@ -26,6 +26,7 @@ GP_MOOD, GP_SE, NN_GP_MOOD, NN_GP_MOOD_CC = 2, 202, 203, 204
 FE, SSP_RK2, SSP_RK3, SSP_RK4 = 8, 9, 10, 12
 HLLC, LLF, HLL, UNSPLIT = 100, 101, 102, 103
 NEUMANN, PERIODIC, REFLECTIVE, DMR = 17, 18, 20, 35
+DIRICHLET, MACH800, DOUBLE_MACH800, RMI, RT, KH = 19, 201, 301, 401, 402, 403  # BC.f90, constants.f90:24-25
 FP_EXACT, FP_FAST = 0, 1
 
 E_ARG, E_CUDA, E_MOOD_CAP, E_DT, E_STATE = -1, -2, -3, -4, -5

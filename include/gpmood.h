@@ -53,6 +53,12 @@ extern "C" {
 #define GPMOOD_PERIODIC    18
 #define GPMOOD_REFLECTIVE  20
 #define GPMOOD_DMR         35
+#define GPMOOD_DIRICHLET   19    /* Shu-Osher inflow/outflow states (BC.f90:61-87) */
+#define GPMOOD_MACH800     201   /* outflow, jet at 0.70 <= x <= 0.80 on y = 0 (BC.f90:137-179) */
+#define GPMOOD_DOUBLE_MACH800 301 /* jets on y = 0 and y = Ly (BC.f90:181-237) */
+#define GPMOOD_RMI         401   /* inflow left, outflow right, reflective top/bottom (BC.f90:239-281) */
+#define GPMOOD_RT          402   /* reflective, hydrostatic ghosts in y, g = 0.1 (BC.f90:343-390) */
+#define GPMOOD_KH          403   /* periodic in x, Neumann in y (BC.f90:392-414) */
 
 /* Floating-point modes of the kernels. */
 #define GPMOOD_FP_EXACT    0     /* reference operation order, no FMA contraction:
@@ -80,7 +86,8 @@ typedef struct gpmood_params {
     int dmp, u2, u2_tol;  /* MOOD checks (logical -> 0/1)              :18-20 */
     int num_flux;         /* GPMOOD_HLLC, _LLF, _HLL, _UNSPLIT         :30 */
     int lf, nf;           /* interior cells in x and y                 :37-38 */
-    int bc_type;          /* GPMOOD_NEUMANN/PERIODIC/REFLECTIVE/DMR    :45 */
+    int bc_type;          /* GPMOOD_NEUMANN/PERIODIC/REFLECTIVE/DMR/DIRICHLET/MACH800/
+                             DOUBLE_MACH800/RMI/RT/KH                    :45 */
     int nmax;             /* step cap of the time loop                 :42 */
     int fp_mode;          /* GPMOOD_FP_EXACT or GPMOOD_FP_FAST */
     int max_mood_iters;   /* MOOD passes allowed per stage before GPMOOD_E_MOOD_CAP; 0 (default)

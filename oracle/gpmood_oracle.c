@@ -563,6 +563,92 @@ void orc_boundary(const orc_params* p, double* U, double t_rk) /* BC.f90:10-421 
                 for (int n = 0; n >= 1 - NGC; n--) p2c(8., 7.1447096, -4.125, 116.5, UP(U, G, l, n));
             }
         }
+    } else if (p->bc_type == 19) { /* Dirichlet :61-87 */
+        for (int n = 1 - NGC; n <= nf + NGC; n++) {
+            for (int l = lf + 1; l <= lf + NGC; l++)
+                p2c(1. + 0.2 * sin(5 * ((l * dx - dx / 2) - 4.5)), 0., 0., 1., UP(U, G, l, n));
+            for (int l = 1 - NGC; l <= 0; l++) p2c(3.857143, 2.629369, 0., 10.33333, UP(U, G, l, n));
+        }
+        for (int l = 1 - NGC; l <= lf + NGC; l++) {
+            for (int n = nf + 1; n <= nf + NGC; n++) memcpy(UP(U, G, l, n), UP(U, G, l, nf), 32);
+            for (int n = 1 - NGC; n <= 0; n++) memcpy(UP(U, G, l, n), UP(U, G, l, 1), 32);
+        }
+    } else if (p->bc_type == 201 || p->bc_type == 301) { /* Mach800_BC :137-179, DoubleMach800_BC :181-237 */
+        for (int n = 1 - NGC; n <= nf + NGC; n++) {
+            for (int l = lf + 1; l <= lf + NGC; l++) memcpy(UP(U, G, l, n), UP(U, G, lf, n), 32);
+            for (int l = 1 - NGC; l <= 0; l++) memcpy(UP(U, G, l, n), UP(U, G, 1, n), 32);
+        }
+        for (int l = 1 - NGC; l <= lf + NGC; l++)
+            for (int n = nf + 1; n <= nf + NGC; n++) memcpy(UP(U, G, l, n), UP(U, G, l, nf), 32);
+        if (p->bc_type == 301)
+            for (int l = 1 - NGC; l <= lf + NGC; l++)
+                for (int n = nf + 1; n <= nf + NGC; n++)
+                    if (fabs((l * dx - dx / 2) - 0.75) <= 0.05) p2c(1.4, 0.0, -800.0, 1.0, UP(U, G, l, n));
+        for (int l = 1 - NGC; l <= lf + NGC; l++)
+            for (int n = 1 - NGC; n <= 0; n++) memcpy(UP(U, G, l, n), UP(U, G, l, 1), 32);
+        for (int l = 1 - NGC; l <= lf + NGC; l++)
+            for (int n = 1 - NGC; n <= 0; n++)
+                if (fabs((l * dx - dx / 2) - 0.75) <= 0.05) p2c(1.4, 0.0, 800.0, 1.0, UP(U, G, l, n));
+    } else if (p->bc_type == 401) { /* RMI_BC :239-281 */
+        for (int n = 1 - NGC; n <= nf + NGC; n++)
+            for (int l = 1 - NGC; l <= 0; l++) p2c(2.666666666666667, 2. * sqrt(1.4), 0., 4.5, UP(U, G, l, n));
+        for (int n = 1 - NGC; n <= nf + NGC; n++)
+            for (int l = lf + 1; l <= lf + NGC; l++) memcpy(UP(U, G, l, n), UP(U, G, lf, n), 32);
+        for (int l = 1 - NGC; l <= lf + NGC; l++) {
+            int k = 0;
+            for (int n = nf + 1; n <= nf + NGC; n++) {
+                memcpy(UP(U, G, l, n), UP(U, G, l, nf - k), 32);
+                k++;
+                UP(U, G, l, n)[MOMY] = -UP(U, G, l, n)[MOMY];
+            }
+            k = 0;
+            for (int n = 0; n >= 1 - NGC; n--) {
+                memcpy(UP(U, G, l, n), UP(U, G, l, 1 + k), 32);
+                k++;
+                UP(U, G, l, n)[MOMY] = -UP(U, G, l, n)[MOMY];
+            }
+        }
+    } else if (p->bc_type == 402) { /* RT_BC :343-390, g = real(0.1, 4) (global_variables.f90:129) */
+        const double grav = (double)0.1f;
+        for (int n = 1 - NGC; n <= nf + NGC; n++) {
+            int k = 0;
+            for (int l = lf + 1; l <= lf + NGC; l++) {
+                memcpy(UP(U, G, l, n), UP(U, G, lf - k, n), 32);
+                k++;
+                UP(U, G, l, n)[MOMX] = -UP(U, G, l, n)[MOMX];
+            }
+            k = 0;
+            for (int l = 0; l >= 1 - NGC; l--) {
+                memcpy(UP(U, G, l, n), UP(U, G, 1 + k, n), 32);
+                k++;
+                UP(U, G, l, n)[MOMX] = -UP(U, G, l, n)[MOMX];
+            }
+        }
+        for (int l = 1 - NGC; l <= lf + NGC; l++) {
+            int k = 0;
+            for (int n = nf + 1; n <= nf + NGC; n++) {
+                const double* q = UP(U, G, l, nf - k);
+                const double pr = orc_pressure(q);
+                p2c(q[RHO], q[MOMX] / q[RHO], -(q[MOMY] / q[RHO]), pr - 2 * k * dy * grav * q[RHO], UP(U, G, l, n));
+                k++;
+            }
+            k = 0;
+            for (int n = 0; n >= 1 - NGC; n--) {
+                const double* q = UP(U, G, l, 1 + k);
+                const double pr = orc_pressure(q);
+                p2c(q[RHO], q[MOMX] / q[RHO], -(q[MOMY] / q[RHO]), pr + 2 * k * dy * grav * q[RHO], UP(U, G, l, n));
+                k++;
+            }
+        }
+    } else if (p->bc_type == 403) { /* KH_BC :392-414: periodic in x, Neumann in y */
+        for (int n = 1 - NGC; n <= nf + NGC; n++) {
+            for (int i = 0; i < NGC; i++) memcpy(UP(U, G, lf + 1 + i, n), UP(U, G, 1 + i, n), 32);
+            for (int i = 0; i < NGC; i++) memcpy(UP(U, G, 1 - NGC + i, n), UP(U, G, lf - NGC + 1 + i, n), 32);
+        }
+        for (int l = 1 - NGC; l <= lf + NGC; l++) {
+            for (int n = nf + 1; n <= nf + NGC; n++) memcpy(UP(U, G, l, n), UP(U, G, l, nf), 32);
+            for (int n = 1 - NGC; n <= 0; n++) memcpy(UP(U, G, l, n), UP(U, G, l, 1), 32);
+        }
     }
 }
 

@@ -42,7 +42,7 @@ def test_default_params_are_the_reference_knobs(pkg):
 
 
 @pytest.mark.parametrize("bad", [dict(mord=7), dict(ngp=6), dict(num_flux=104), dict(integrator=11),
-                                 dict(bc_type=19), dict(lf=2), dict(method=200), dict(fp_mode=3),
+                                 dict(bc_type=21), dict(lf=2), dict(method=200), dict(method=204), dict(fp_mode=3),
                                  dict(max_mood_iters=-1), dict(cfl=0.0)])
 def test_invalid_knobs_rejected(pkg, bad):
     with pytest.raises(pkg.GpmoodError) as e:

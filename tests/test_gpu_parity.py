@@ -135,7 +135,8 @@ def test_run_stops_at_tmax(pkg, oracle):
 
 def test_boundary_c_matches_oracle(pkg, oracle):
     rng = np.random.default_rng(0)
-    for bc, lx, ly in ((17, 1., 1.), (18, 1., 1.), (20, 1., 1.), (35, 4., 1.)):
+    for bc, lx, ly in ((17, 1., 1.), (18, 1., 1.), (20, 1., 1.), (35, 4., 1.), (19, 9., 1.), (201, 1.5, 1.5),
+                       (301, 1.5, 1.5), (401, 6., 1.), (402, 0.25, 1.), (403, 1., 1.)):
         p = oracle.make_params(40, 24, bc=bc, lx=lx, ly=ly)
         U = rng.uniform(0.5, 2.0, size=oracle.padded(40, 24).shape)
         Ug = U.copy()
@@ -231,3 +232,28 @@ def test_inadmissible_state_is_caught_and_reported(pkg, oracle, bad):
     interior = out[4:-4, 4:-4]
     bad_cells = ~np.isfinite(interior).all(axis=-1)
     assert bad_cells.any() and bad_cells.sum() < 50  # local, not spread over the grid
+
+
+@pytest.mark.parametrize("bc,lx,ly", [(19, 9., 1.), (201, 1.5, 1.5), (301, 1.5, 1.5), (401, 6., 1.), (402, 0.25, 1.),
+                                      (403, 1., 1.)])
+def test_other_boundary_types_step_like_the_oracle(pkg, oracle, bc, lx, ly):
+    """Dirichlet, Mach800, DoubleMach800, RMI, RT and KH boundaries (BC.f90)
+    through whole steps: time steps and states bit-identical to the oracle."""
+    lf, nf = 48, 32
+    p = oracle.make_params(lf, nf, bc=bc, lx=lx, ly=ly, tmax=1.0)
+    U = oracle.initial_condition(p, "rp2d3")
+    st = oracle.Stepper(p)
+    Ug = U.copy()
+    t = 0.0
+    with pkg.Solver(lf=lf, nf=nf, bc_type=bc, lx=lx, ly=ly, tmax=1.0, fp_mode=pkg.FP_EXACT) as s:
+        for step in range(3):
+            dt = oracle.setdt(p, U, p.tmax - t)
+            dtg = s.Setdt(Ug, p.tmax - t)
+            assert dtg == dt, (step, dtg, dt)
+            Ur = np.empty_like(U)
+            st.time_stepping(U, Ur, t, dt)
+            Ugr = np.empty_like(Ug)
+            s.time_stepping(Ug, Ugr, t, dtg)
+            assert nan_equal(Ugr, Ur), (step, np.nanmax(np.abs(Ugr - Ur)))
+            t += dt
+            U, Ug = Ur, Ugr
