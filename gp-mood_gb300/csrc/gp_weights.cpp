@@ -131,6 +131,25 @@ void gauss_rule(int ngp, f128* pt, double* w) {
 
 double gpm_cell_size(double length, int n) { return (double)((_Float128)length / n); }
 
+// pol_presim (GP_init.f90:359-419): the third-order polynomial weights of
+// POL_MOOD / Unlim_POL replace the order-3 GP weights, 2 Gauss points per
+// face, over the 5-point stencil (M, L, T, R, B); o3_coef is constants.f90:61.
+// Order 1 keeps the weight 1.
+extern "C" void gpm_pol_weights(GpWeights* w) {
+    const double c[5] = {15. / 18, 1. / 3, 1. / (4 * sqrt(3.)), -1. / (4 * sqrt(3.)), -1. / 6};
+    // kM, kCloseNrm, kCloseTrans, kFarTrans, kFarNrm = 0..4; [face iL, iT, iR, iB][gauss point][stencil point]
+    static const int k[4][2][5] = {{{0, 1, 3, 4, 2}, {0, 1, 2, 4, 3}},
+                                   {{0, 2, 1, 3, 4}, {0, 3, 1, 2, 4}},
+                                   {{0, 4, 3, 1, 2}, {0, 4, 2, 1, 3}},
+                                   {{0, 2, 4, 3, 1}, {0, 3, 4, 2, 1}}};
+    for (int f = 0; f < 4; f++)
+        for (int g = 0; g < 2; g++) {
+            for (int m = 0; m < 13; m++) w->zt[1][f][g][m] = 0.0;
+            for (int m = 0; m < 5; m++) w->zt[1][f][g][m] = c[k[f][g][m]];
+            w->zt[0][f][g][0] = 1.0;
+        }
+}
+
 extern "C" int gpm_gp_presim(double ell_o_dx, double lx, double ly, int lf, int nf, int mord, int ngp,
                              GpWeights* out, double inv_err[3]) {
     if (!(mord == 1 || mord == 3 || mord == 5) || ngp < 1 || ngp > GPM_MAXGP || lf < 1 || nf < 1)

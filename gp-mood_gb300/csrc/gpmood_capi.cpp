@@ -61,6 +61,7 @@ struct gpmood_ctx {
 };
 
 double gpm_probe_fp64();
+extern "C" void gpm_pol_weights(GpWeights* w);
 int gpm_fast_rcp_dev(const double* x, double* y, int n);
 
 int gpm_mood_solo_default() {
@@ -345,9 +346,12 @@ int validate(const gpmood_params* p, char* why, size_t n) {
         p->integrator != GPMOOD_SSP_RK4) {
         snprintf(why, n, "integrator %d unsupported (FE=8, SSP_RK2=9, SSP_RK3=10, SSP_RK4=12)", p->integrator); return -1; }
     if (p->method != GPMOOD_GP_MOOD && p->method != GPMOOD_GP_SE && p->method != GPMOOD_NN_GP_MOOD &&
-        p->method != GPMOOD_NN_GP_MOOD_CC) {
-        snprintf(why, n, "method %d unsupported (GP_MOOD=2, GP_SE=202, NN_GP_MOOD=203, NN_GP_MOOD_CC=204)", p->method);
+        p->method != GPMOOD_NN_GP_MOOD_CC && p->method != GPMOOD_POL_MOOD && p->method != GPMOOD_UNLIM_POL) {
+        snprintf(why, n, "method %d unsupported (GP_MOOD=2, POL_MOOD=200, Unlim_POL=201, GP_SE=202, NN_GP_MOOD=203, "
+                 "NN_GP_MOOD_CC=204)", p->method);
         return -1; }
+    if ((p->method == GPMOOD_POL_MOOD || p->method == GPMOOD_UNLIM_POL) && (p->mord != 3 || p->ngp != 2)) {
+        snprintf(why, n, "POL_MOOD and Unlim_POL need Mord 3 and ngp 2 (pol_presim's weights)"); return -1; }
     if (p->method == GPMOOD_NN_GP_MOOD_CC && p->mord != 3) {  // mod_NN_GP_MOOD_CC.f90:73 stops above order 3
         snprintf(why, n, "NN_GP_MOOD_CC needs Mord 3"); return -1; }
     if (p->num_flux < GPMOOD_HLLC || p->num_flux > GPMOOD_UNSPLIT) {
@@ -428,6 +432,9 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
         c->p.method = GPMOOD_NN_GP_MOOD;
         c->p.nn_reference = 1;
     }
+    // POL_MOOD / Unlim_POL: GP_MOOD / GP_SE with the polynomial weights (below)
+    const bool pol = p->method == GPMOOD_POL_MOOD || p->method == GPMOOD_UNLIM_POL;
+    if (pol) c->p.method = p->method == GPMOOD_POL_MOOD ? GPMOOD_GP_MOOD : GPMOOD_GP_SE;
     c->g.lf = p->lf;
     c->g.nf = p->nf;
     c->g.nx = p->lf + 2 * GPM_NGC;
@@ -456,6 +463,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
         delete c;
         return fail(nullptr, GPMOOD_E_ARG, "GP precompute rejected the knobs");
     }
+    if (pol) gpm_pol_weights(&c->w);
     int ndev = 0;
     cudaError_t e = cudaGetDeviceCount(&ndev);
     if (e != cudaSuccess || ndev < 1) {
@@ -587,6 +595,7 @@ int gpmood_gp_weights(const gpmood_params* p, double* zt, double* d2, double* in
     double ie[3];
     if (gpm_gp_presim(p->ell_o_dx, p->lx, p->ly, p->lf, p->nf, p->mord, p->ngp, &w, ie))
         return fail(nullptr, GPMOOD_E_ARG, "GP precompute rejected the knobs");
+    if (p->method == GPMOOD_POL_MOOD || p->method == GPMOOD_UNLIM_POL) gpm_pol_weights(&w);
     const int ngp = p->ngp;
     if (zt)
         for (int o = 0; o < 3; o++)

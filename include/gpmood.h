@@ -39,6 +39,10 @@ extern "C" {
 #define GPMOOD_GP_MOOD     2     /* method: GP-MOOD */
 #define GPMOOD_GP_SE       202   /* method: unlimited GP (MOOD off) */
 #define GPMOOD_NN_GP_MOOD  203   /* method: GP-MOOD with the MLP a-priori gate */
+#define GPMOOD_POL_MOOD    200   /* method: MOOD with the third-order polynomial reconstruction
+                                    (mod_pol_MOOD.f90, pol_presim); Mord 3, ngp 2 */
+#define GPMOOD_UNLIM_POL   201   /* method: the same polynomial reconstruction without MOOD
+                                    (mod_Unlim_Pol.f90); Mord 3, ngp 2 */
 #define GPMOOD_NN_GP_MOOD_CC 204 /* method: the reference's network with its convex-combination
                                     reconstruction (mod_NN_GP_MOOD_CC.f90); Mord 3 */
 #define GPMOOD_FE          8     /* integrator: Forward_Euler */

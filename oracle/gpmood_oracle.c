@@ -713,6 +713,25 @@ orc_ctx* orc_create(const orc_params* p)
     if (!c) return NULL;
     c->p = *p;
     if (orc_gp_presim(p, &c->gp) != 0) { free(c); return NULL; }
+    if (p->method == 200 || p->method == 201) {
+        /* POL_MOOD_ / Unlim_POL_ (mod_pol_MOOD.f90, mod_Unlim_Pol.f90): the
+         * weights of pol_presim (GP_init.f90:359-419) at order 3, o3_coef of
+         * constants.f90:61, Pol_zT_o3(point, face, gauss point); the stepping
+         * is GP_MOOD's (DETECTION on) or GP_SE's (none). */
+        const double oc[5] = {15. / 18, 1. / 3, 1. / (4 * sqrt(3.)), -1. / (4 * sqrt(3.)), -1. / 6};
+        enum { M = 0, CN = 1, CT = 2, FT = 3, FN = 4 };
+        const int tab[4][2][5] = {{{M, CN, FT, FN, CT}, {M, CN, CT, FN, FT}},  /* iL */
+                                  {{M, CT, CN, FT, FN}, {M, FT, CN, CT, FN}},  /* iT */
+                                  {{M, FN, FT, CN, CT}, {M, FN, CT, CN, FT}},  /* iR */
+                                  {{M, CT, FN, FT, CN}, {M, FT, FN, CT, CN}}}; /* iB */
+        for (int f = 0; f < 4; f++)
+            for (int j = 0; j < 2; j++) {
+                for (int m = 0; m < 13; m++) c->gp.zt[1][f][j][m] = 0.0;
+                for (int m = 0; m < 5; m++) c->gp.zt[1][f][j][m] = oc[tab[f][j][m]];
+                c->gp.zt[0][f][j][0] = 1.0;
+            }
+        c->p.method = p->method == 200 ? 2 : 202;
+    }
     c->G = mkgrid(p);
     c->dx = dx_of(p);
     c->dy = dy_of(p);

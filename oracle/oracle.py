@@ -77,6 +77,8 @@ def lib() -> C.CDLL:
         L.orc_create.restype = C.c_void_p
         L.orc_destroy.argtypes = [C.c_void_p]
         L.orc_set_cc.argtypes = [C.c_void_p, C.c_int, C.c_void_p]
+        L.orc_weights.argtypes = [C.c_void_p]
+        L.orc_weights.restype = C.c_void_p
         L.orc_time_stepping.argtypes = [C.c_void_p, dp, dp, C.c_double, C.c_double, C.c_void_p, C.c_void_p,
                                         P(C.c_longlong)]
         L.orc_shock_detector.argtypes = [P(OrcParams), dp, C.c_int, C.c_int]
@@ -144,6 +146,10 @@ class Stepper:
 
     def __del__(self):
         self.close()
+
+    def weights(self) -> OrcGp:
+        """The weights the context steps with (GP, or pol_presim's for POL_MOOD / Unlim_POL)."""
+        return OrcGp.from_address(lib().orc_weights(self._h))
 
     def set_cc(self, col: int, w=None):
         """NN_GP_MOOD_CC_ blend of column `col` with row pairs w[nf+2, 2] (None: off)."""

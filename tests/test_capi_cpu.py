@@ -6,6 +6,7 @@ import ctypes as C
 import re
 from pathlib import Path
 
+import numpy as np
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
@@ -63,3 +64,21 @@ def test_no_gpu_means_error_not_fallback(pkg):
     with pytest.raises(pkg.GpmoodError) as e:
         pkg.Solver(lf=32, nf=32)
     assert e.value.code == -2
+
+
+def test_polynomial_weights_match_the_oracle(pkg, oracle):
+    """POL_MOOD / Unlim_POL (pol_presim, GP_init.f90:359-419): the host library's
+    order-3 weights equal the oracle's, sum to one and mirror L/R, T/B."""
+    from gpmood_gb300.gpmood import gp_weights
+    for method in (200, 201):
+        zt, _, _ = gp_weights(pkg.default_params(lf=32, nf=32, mord=3, ngp=2, method=method))
+        st = oracle.Stepper(oracle.make_params(32, 32, mord=3, ngp=2, method=method))
+        zo = np.array(st.weights().zt, dtype=np.float64).reshape(3, 4, 5, 13)
+        assert np.array_equal(zt[1], zo[1, :, :2, :])
+        assert np.all(zt[0, :, :, 0] == 1.0)
+        assert np.allclose(zt[1, :, :, :5].sum(axis=-1), 1.0, atol=1e-15)
+        iL, iT, iR, iB = 0, 1, 2, 3  # stencil points M, L, T, R, B = 0..4
+        assert np.array_equal(zt[1, iL, :, [0, 1, 2, 3, 4]], zt[1, iR, :, [0, 3, 2, 1, 4]])
+        assert np.array_equal(zt[1, iT, :, [0, 1, 2, 3, 4]], zt[1, iB, :, [0, 1, 4, 3, 2]])
+    with pytest.raises(pkg.GpmoodError):
+        gp_weights(pkg.default_params(lf=32, nf=32, mord=5, ngp=2, method=200))

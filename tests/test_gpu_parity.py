@@ -24,6 +24,9 @@ CASES = {
     "ragged_periodic": ("vortex", 33, 41, dict(bc=18, lx=10.0, ly=10.0, tmax=1.0)),
     # smaller than one tile in both directions
     "tiny": ("rp2d3", 8, 6, dict(bc=17, tmax=0.8)),
+    # the polynomial reconstruction of pol_presim with and without MOOD (method 200, 201)
+    "pol_mood": ("rp2d3", 48, 48, dict(bc=17, tmax=0.8, mord=3, ngp=2, method=200)),
+    "unlim_pol": ("vortex", 48, 48, dict(bc=18, lx=10.0, ly=10.0, tmax=1.0, mord=3, ngp=2, method=201)),
 }
 
 
