@@ -102,8 +102,8 @@ def harvest(runs, capacity: int, keep_negative: float, steps_per_run: int, seed:
 
 
 def training_runs(seed: int = 0, sedov_n: int = 2048, rp_n: int = 256):
-    """The seeded runs of the design: the 2DRP3 IC (configs[0]) and the Sedov
-    IC with rho, p and E0 perturbed by up to +-20 %."""
+    """The seeded training runs: the 2DRP3 IC at 256^2 and the Sedov IC with
+    rho, p and E0 perturbed by up to +-20 %."""
     rng = np.random.default_rng(seed)
     runs = [(ic.rp2d3(rp_n, rp_n), dict(lf=rp_n, nf=rp_n, bc_type=17, tmax=0.8))]
     for _ in range(4):

@@ -208,8 +208,8 @@ def test_one_call_step_equals_the_two_calls(pkg, oracle):
 
 @pytest.mark.parametrize("bad", ["negative_pressure", "nan_density"])
 def test_inadmissible_state_is_caught_and_reported(pkg, oracle, bad):
-    """An inadmissible cell planted in the initial array (SURVEY-style fault
-    injection on the host): MOOD lowers the cells around it to first order,
+    """An inadmissible cell planted in the initial array (fault injection on
+    the host, no GPU fault): MOOD lowers the cells around it to first order,
     the bad values stay in order-1 cells, the step equals the oracle bit for
     bit, and status bit 0 reports the state left in an order-1 cell without
     failing the call."""
