@@ -9,11 +9,11 @@ Package layout:
   ic.py        initial conditions of the benchmark problems
   build.py     in-tree build of libgpmood.so
 """
-from .gpmood import (DIRICHLET, DMR, DOUBLE_MACH800, FE, KH, MACH800, RMI, RT, FP_EXACT, FP_FAST, GP_MOOD, GP_SE, HLL, HLLC, LLF, NEUMANN, NGC, NN_GP_MOOD,
+from .gpmood import (DIRICHLET, DMR, DOUBLE_MACH800, FE, FOG, KH, MACH800, RMI, RT, FP_EXACT, FP_FAST, GP_MOOD, GP_SE, HLL, HLLC, LLF, NEUMANN, NGC, NN_GP_MOOD,
                      NN_GP_MOOD_CC, POL_MOOD, UNLIM_POL,
                      PERIODIC, REFLECTIVE, SSP_RK2, SSP_RK3, SSP_RK4, UNSPLIT, Adjoint, Batch, GpmoodError, Params,
                      Solver, default_params, gp_weights, load_library, padded, probe_fp64)
 
-__all__ = ["DIRICHLET", "DMR", "DOUBLE_MACH800", "FE", "KH", "MACH800", "RMI", "RT", "FP_EXACT", "FP_FAST", "GP_MOOD", "GP_SE", "HLL", "HLLC", "LLF", "NEUMANN", "NGC",
+__all__ = ["DIRICHLET", "DMR", "DOUBLE_MACH800", "FE", "FOG", "KH", "MACH800", "RMI", "RT", "FP_EXACT", "FP_FAST", "GP_MOOD", "GP_SE", "HLL", "HLLC", "LLF", "NEUMANN", "NGC",
            "NN_GP_MOOD", "NN_GP_MOOD_CC", "POL_MOOD", "UNLIM_POL", "PERIODIC", "REFLECTIVE", "SSP_RK2", "SSP_RK3", "SSP_RK4", "UNSPLIT", "Adjoint", "Batch",
            "GpmoodError", "Params", "Solver", "default_params", "gp_weights", "load_library", "padded", "probe_fp64"]

@@ -346,10 +346,13 @@ int validate(const gpmood_params* p, char* why, size_t n) {
         p->integrator != GPMOOD_SSP_RK4) {
         snprintf(why, n, "integrator %d unsupported (FE=8, SSP_RK2=9, SSP_RK3=10, SSP_RK4=12)", p->integrator); return -1; }
     if (p->method != GPMOOD_GP_MOOD && p->method != GPMOOD_GP_SE && p->method != GPMOOD_NN_GP_MOOD &&
-        p->method != GPMOOD_NN_GP_MOOD_CC && p->method != GPMOOD_POL_MOOD && p->method != GPMOOD_UNLIM_POL) {
-        snprintf(why, n, "method %d unsupported (GP_MOOD=2, POL_MOOD=200, Unlim_POL=201, GP_SE=202, NN_GP_MOOD=203, "
-                 "NN_GP_MOOD_CC=204)", p->method);
+        p->method != GPMOOD_NN_GP_MOOD_CC && p->method != GPMOOD_POL_MOOD && p->method != GPMOOD_UNLIM_POL &&
+        p->method != GPMOOD_FOG) {
+        snprintf(why, n, "method %d unsupported (FOG=1, GP_MOOD=2, POL_MOOD=200, Unlim_POL=201, GP_SE=202, "
+                 "NN_GP_MOOD=203, NN_GP_MOOD_CC=204)", p->method);
         return -1; }
+    if (p->method == GPMOOD_FOG && p->ngp != 1) {  // FOG_ sets Gauss point 1 only (mod_FOG.f90:22-24)
+        snprintf(why, n, "FOG needs ngp 1"); return -1; }
     if ((p->method == GPMOOD_POL_MOOD || p->method == GPMOOD_UNLIM_POL) && (p->mord != 3 || p->ngp != 2)) {
         snprintf(why, n, "POL_MOOD and Unlim_POL need Mord 3 and ngp 2 (pol_presim's weights)"); return -1; }
     if (p->method == GPMOOD_NN_GP_MOOD_CC && p->mord != 3) {  // mod_NN_GP_MOOD_CC.f90:73 stops above order 3
@@ -435,6 +438,13 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     // POL_MOOD / Unlim_POL: GP_MOOD / GP_SE with the polynomial weights (below)
     const bool pol = p->method == GPMOOD_POL_MOOD || p->method == GPMOOD_UNLIM_POL;
     if (pol) c->p.method = p->method == GPMOOD_POL_MOOD ? GPMOOD_GP_MOOD : GPMOOD_GP_SE;
+    // FOG: every face state is the cell value and no DETECTION runs (mod_FOG.f90,
+    // mod_FE.f90:161), i.e. GP_SE at order 1 (its weight is 1); the order mask
+    // then reads 1 where the reference's CellGPO keeps Mord untouched
+    if (p->method == GPMOOD_FOG) {
+        c->p.method = GPMOOD_GP_SE;
+        c->p.mord = 1;
+    }
     c->g.lf = p->lf;
     c->g.nf = p->nf;
     c->g.nx = p->lf + 2 * GPM_NGC;
@@ -444,7 +454,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     c->g.dy = (double)((_Float128)p->ly / p->nf);
     c->g.bc_type = p->bc_type;
     c->g.ngp = p->ngp;
-    c->g.mord = p->mord;
+    c->g.mord = c->p.mord;
     c->g.method = c->p.method;
     c->g.num_flux = p->num_flux;
     c->g.mood_solo = gpm_mood_solo_default();
@@ -536,7 +546,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
         cudaMemsetAsync(c->dFx, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dFy, 0, sb, s0) != cudaSuccess ||
         cudaMemsetAsync(c->dU, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dUr, 0, sb, s0) != cudaSuccess ||
         cudaMemsetAsync(c->dU1, 0, sb, s0) != cudaSuccess || cudaMemsetAsync(c->dU2, 0, sb, s0) != cudaSuccess ||
-        cudaMemsetAsync(c->dStageOrd, p->mord, GPM_MAXST * c->ncell, s0) != cudaSuccess ||
+        cudaMemsetAsync(c->dStageOrd, c->p.mord, GPM_MAXST * c->ncell, s0) != cudaSuccess ||
         cudaMemsetAsync(c->dBar, 0, sizeof(GridBar), s0) != cudaSuccess ||
         cudaStreamSynchronize(s0) != cudaSuccess) {
         fail(c, GPMOOD_E_CUDA, "device initialisation failed");

@@ -24,6 +24,7 @@ NGC = 4
 # gp-mood-code/constants.f90:17-34
 GP_MOOD, GP_SE, NN_GP_MOOD, NN_GP_MOOD_CC = 2, 202, 203, 204
 POL_MOOD, UNLIM_POL = 200, 201  # mod_pol_MOOD.f90, mod_Unlim_Pol.f90: Mord 3, ngp 2
+FOG = 1  # mod_FOG.f90: first-order Godunov, ngp 1
 FE, SSP_RK2, SSP_RK3, SSP_RK4 = 8, 9, 10, 12
 HLLC, LLF, HLL, UNSPLIT = 100, 101, 102, 103
 NEUMANN, PERIODIC, REFLECTIVE, DMR = 17, 18, 20, 35
@@ -361,7 +362,7 @@ class Solver:
         from . import snapshot
         U, t, n = self.get_state()
         method = {GP_MOOD: "GP_MOOD", GP_SE: "GP_SE", NN_GP_MOOD: "NN_GP_MOOD", NN_GP_MOOD_CC: "NN_GP_MOOD_CC",
-                  POL_MOOD: "POL_MOOD", UNLIM_POL: "Unlim_POL"}.get(self.p.method, str(self.p.method))
+                  POL_MOOD: "POL_MOOD", UNLIM_POL: "Unlim_POL", FOG: "FOG"}.get(self.p.method, str(self.p.method))
         snapshot.save_snapshot(path, U, t, n, self.orders(), cfl=self.p.cfl, problem=problem, method=method,
                                nn_filename=nn_filename)
 

@@ -36,6 +36,7 @@ extern "C" {
 #endif
 
 /* Enumerations share the reference's values (gp-mood-code/constants.f90:17-34). */
+#define GPMOOD_FOG         1     /* method: first-order Godunov (mod_FOG.f90); ngp 1 */
 #define GPMOOD_GP_MOOD     2     /* method: GP-MOOD */
 #define GPMOOD_GP_SE       202   /* method: unlimited GP (MOOD off) */
 #define GPMOOD_NN_GP_MOOD  203   /* method: GP-MOOD with the MLP a-priori gate */
@@ -84,7 +85,8 @@ typedef struct gpmood_params {
     double lx, ly;        /* domain [0,Lx]x[0,Ly] (Lx_16, Ly_16)       :43-44 */
     double tmax;          /* final time                                :41 */
     int integrator;       /* GPMOOD_FE, _SSP_RK2, _SSP_RK3, _SSP_RK4   :9  */
-    int method;           /* GPMOOD_GP_MOOD, GPMOOD_GP_SE, GPMOOD_NN_GP_MOOD, GPMOOD_NN_GP_MOOD_CC */
+    int method;           /* GPMOOD_FOG, GPMOOD_GP_MOOD, GPMOOD_POL_MOOD, GPMOOD_UNLIM_POL, GPMOOD_GP_SE,
+                             GPMOOD_NN_GP_MOOD, GPMOOD_NN_GP_MOOD_CC */
     int mord;             /* maximal order 1, 3 or 5                   :15 */
     int ngp;              /* Gauss points per face, 1..5               :16 */
     int dmp, u2, u2_tol;  /* MOOD checks (logical -> 0/1)              :18-20 */

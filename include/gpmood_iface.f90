@@ -16,7 +16,8 @@ module gpmood_iface
    implicit none
 
    integer(c_int), parameter :: GPMOOD_GP_MOOD = 2, GPMOOD_GP_SE = 202, GPMOOD_NN_GP_MOOD = 203, &
-                                GPMOOD_NN_GP_MOOD_CC = 204, GPMOOD_POL_MOOD = 200, GPMOOD_UNLIM_POL = 201
+                                GPMOOD_NN_GP_MOOD_CC = 204, GPMOOD_POL_MOOD = 200, GPMOOD_UNLIM_POL = 201, &
+                                GPMOOD_FOG = 1
    integer(c_int), parameter :: GPMOOD_SSP_RK3 = 10, GPMOOD_HLLC = 100
    integer(c_int), parameter :: GPMOOD_NEUMANN = 17, GPMOOD_PERIODIC = 18, GPMOOD_REFLECTIVE = 20, GPMOOD_DMR = 35
    integer(c_int), parameter :: GPMOOD_FP_EXACT = 0, GPMOOD_FP_FAST = 1

@@ -732,6 +732,10 @@ orc_ctx* orc_create(const orc_params* p)
             }
         c->p.method = p->method == 200 ? 2 : 202;
     }
+    if (p->method == 1) { /* FOG_ (mod_FOG.f90): Uh = Uin, no DETECTION: GP_SE at order 1 */
+        c->p.method = 202;
+        c->p.mord = 1;
+    }
     c->G = mkgrid(p);
     c->dx = dx_of(p);
     c->dy = dy_of(p);

@@ -33,7 +33,8 @@ typedef struct orc_params {
     double tmax;
     int mord;          /* 1, 3 or 5 */
     int ngp;           /* Gauss points per face, 1..5 */
-    int method;        /* 2 = GP_MOOD, 202 = GP_SE, 200 = POL_MOOD, 201 = Unlim_POL (constants.f90:17);
+    int method;        /* 1 = FOG (ngp 1), 2 = GP_MOOD, 202 = GP_SE, 200 = POL_MOOD, 201 = Unlim_POL
+                          (constants.f90:17);
                           POL_MOOD/Unlim_POL need mord 3 and ngp 2 */
     int dmp, u2, u2_tol;
     int lf, nf;        /* interior cells */
