@@ -93,3 +93,21 @@ def test_shu_osher_left_state_is_the_dirichlet_inflow(oracle):
     p = oracle.make_params(36, 4, bc=19, lx=9.0, ly=1.0)
     oracle.boundary(p, V)
     assert np.array_equal(V[NGC + 1, 0], U[NGC + 1, NGC])  # ghost (l = -3) = first cell, both p2c(3.857143, ...)
+
+
+@pytest.mark.parametrize("name,oname,lx,ly", [("rp2d3", "rp2d3", 1.0, 1.0), ("sedov", "sedov", 1.0, 1.0),
+                                             ("dmr", "dmr", 4.0, 1.0), ("isentropic_vortex", "vortex", 10.0, 10.0)])
+def test_builders_match_the_oracle_ics(oracle, name, oname, lx, ly):
+    """ic.py's builders followed by Boundary_C (main.f90:125) equal the CPU
+    restatement's initial states (IC.f90 plus Boundary_C); the vortex's exp
+    and power agree to a few ulp."""
+    ic = _ic()
+    lf, nf = 40, 24
+    p = oracle.make_params(lf, nf, lx=lx, ly=ly, bc={"dmr": 35, "vortex": 18}.get(oname, 17))
+    Uo = oracle.initial_condition(p, oname)
+    Ui = getattr(ic, name)(lf, nf, lx=lx, ly=ly)
+    oracle.boundary(p, Ui)
+    if name in ("rp2d3", "dmr"):
+        assert np.array_equal(Ui, Uo)
+    else:
+        np.testing.assert_allclose(Ui, Uo, rtol=1e-14, atol=1e-14)
