@@ -6,6 +6,7 @@
 // 4-byte troubled-cell count per MOOD pass.
 #include <cuda_runtime.h>
 #include <math.h>
+#include <nvtx3/nvToolsExt.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -74,6 +75,15 @@ int gpm_mood_solo_default() {
 
 namespace {
 
+// NVTX range over a host scope (steps and stages show up on an Nsight Systems
+// timeline; without a tool attached the calls do nothing).
+struct NvtxRange {
+    explicit NvtxRange(const char* name) { nvtxRangePushA(name); }
+    ~NvtxRange() { nvtxRangePop(); }
+    NvtxRange(const NvtxRange&) = delete;
+    NvtxRange& operator=(const NvtxRange&) = delete;
+};
+
 thread_local char g_err[512];
 
 int fail(gpmood_ctx* c, int code, const char* fmt, ...) {
@@ -123,6 +133,9 @@ StageArgs stage_args(gpmood_ctx* c, const double* uin, double* uout, int stage, 
 // for time-dependent boundaries (0: t, 1: t+dt, 2: t+dt/2).  Nothing here
 // waits for the GPU: pass counts and status come back once per step.
 int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, int bc_stage) {
+    static const char* const kName[GPM_MAXST] = {"Forward_Euler 1", "Forward_Euler 2", "Forward_Euler 3",
+                                                 "Forward_Euler 4", "Forward_Euler 5"};
+    NvtxRange range(kName[stage < GPM_MAXST ? stage : GPM_MAXST - 1]);
     cudaStream_t s = c->stream;
     const KernelTable& kt = *c->kt;
     cudaEvent_t* ev = c->ev[stage];
@@ -253,6 +266,7 @@ int run_rk4(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
 // the next step's Setdt into the final combination.  One host
 // synchronisation per step, at its end.
 int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
+    NvtxRange range("time_stepping");
     cudaStream_t s = c->stream;
     CU(cudaMemsetAsync(&c->dSc->detected_step, 0, 2 * sizeof(unsigned long long), s));
     CU(cudaMemsetAsync(&c->dSc->status, 0, sizeof(int), s));  // this step's flags (counters keep them all)
