@@ -72,6 +72,8 @@ struct GridGeom {
     double dx, dy;
     int bc_type, ngp, mord, method;
     int dmp, u2, u2_tol;
+    int u2_fd;           // POL_MOOD: the U2 test's second derivatives are the 3-point differences
+                         // D2O2/dx^2 (mod_subroutine_MOOD.f90:81-84) instead of the GP weights
     int num_flux;        // 100 HLLC, 101 LLF, 102 HLL, 103 unsplit
     int mood_solo;       // device MOOD loop: lists of at most this many cells run in one CTA
     int cc_col;          // NN_GP_MOOD_CC: the column l whose order-3 states are blended (-1: none)

@@ -477,6 +477,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     c->g.dmp = p->dmp;
     c->g.u2 = p->u2;
     c->g.u2_tol = p->u2_tol;
+    c->g.u2_fd = p->method == GPMOOD_POL_MOOD;
     c->ncell = (size_t)c->g.nx * c->g.ny;
     c->kt = p->fp_mode == GPMOOD_FP_FAST ? &gpm_fast::table : &gpm_exact::table;
     {

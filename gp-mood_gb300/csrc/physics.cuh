@@ -476,20 +476,32 @@ __device__ __forceinline__ bool mood_troubled(const Cell& uo, const double* __re
     // 5 cross cells, each from that cell's own 5-point cross.
     double D2x[5], D2y[5];
     const int ci_[5] = {-1, 0, 1, 0, 0}, cj_[5] = {0, 0, 0, -1, 1};  // (-1,0),(0,0),(1,0),(0,-1),(0,1)
+    if (g.u2_fd) {
+        // POL_MOOD (:81-84): dot_product((1,-2,1), rho(l+i-1:l+i+1, n+j))/dx**2;
+        // 1*a and -2*b are exact, so the sum is (a - 2b) + c in either FP mode.
 #pragma unroll
-    for (int s = 0; s < 5; s++) {
-        const double* base = uin + (ptrdiff_t)4 * ci_[s] + (ptrdiff_t)row * cj_[s];
-        double q[5];
-#pragma unroll
-        for (int k = 0; k < 5; k++) q[k] = __ldg(base + (ptrdiff_t)4 * st_ox(k) + (ptrdiff_t)row * st_oy(k));
-        double sx = d2x[0] * q[0], sy = d2y[0] * q[0];
-#pragma unroll
-        for (int k = 1; k < 5; k++) {
-            sx = sx + d2x[k] * q[k];
-            sy = sy + d2y[k] * q[k];
+        for (int s = 0; s < 5; s++) {
+            const double* base = uin + (ptrdiff_t)4 * ci_[s] + (ptrdiff_t)row * cj_[s];
+            const double m = __ldg(base);
+            D2x[s] = ((__ldg(base - 4) + -2. * m) + __ldg(base + 4)) / (g.dx * g.dx);
+            D2y[s] = ((__ldg(base - row) + -2. * m) + __ldg(base + row)) / (g.dy * g.dy);
         }
-        D2x[s] = sx;
-        D2y[s] = sy;
+    } else {
+#pragma unroll
+        for (int s = 0; s < 5; s++) {
+            const double* base = uin + (ptrdiff_t)4 * ci_[s] + (ptrdiff_t)row * cj_[s];
+            double q[5];
+#pragma unroll
+            for (int k = 0; k < 5; k++) q[k] = __ldg(base + (ptrdiff_t)4 * st_ox(k) + (ptrdiff_t)row * st_oy(k));
+            double sx = d2x[0] * q[0], sy = d2y[0] * q[0];
+#pragma unroll
+            for (int k = 1; k < 5; k++) {
+                sx = sx + d2x[k] * q[k];
+                sy = sy + d2y[k] * q[k];
+            }
+            D2x[s] = sx;
+            D2y[s] = sy;
+        }
     }
     const double Xmin = fmin(fmin(fmin(fmin(D2x[0], D2x[1]), D2x[2]), D2x[3]), D2x[4]);
     const double Xmax = fmax(fmax(fmax(fmax(D2x[0], D2x[1]), D2x[2]), D2x[3]), D2x[4]);

@@ -1164,7 +1164,7 @@ __device__ __forceinline__ GridGeom bgeom(const BatchArgs& a, const BProb& p) {
     g.lf = p.lf; g.nf = p.nf; g.nx = p.nx; g.ny = p.ny;
     g.dx = p.dx; g.dy = p.dy;
     g.bc_type = a.bc_type; g.ngp = a.ngp; g.mord = a.mord; g.method = a.method;
-    g.dmp = a.dmp; g.u2 = a.u2; g.u2_tol = a.u2_tol; g.num_flux = a.num_flux;
+    g.dmp = a.dmp; g.u2 = a.u2; g.u2_tol = a.u2_tol; g.u2_fd = 0; g.num_flux = a.num_flux;
     g.mood_solo = a.mood_solo;
     g.cc_col = -1;
     return g;

@@ -656,13 +656,20 @@ double orc_setdt(const orc_params* p, const double* U, double dtfinal) /* physic
 {
     grid G = mkgrid(p);
     const double dx = dx_of(p), dy = dy_of(p);
+    /* deprecated/physics.f90:94-97: dx0 = Lx/lf0 in double */
+    const int reduce = p->setdt_kind == 1 && p->lf0 > 0 && p->nf0 > 0;
+    const double dx0 = reduce ? p->lx / p->lf0 : dx, dy0 = reduce ? p->ly / p->nf0 : dy;
     double dt = 1.0e30;
     for (int n = 1 - NGC; n <= p->nf + NGC; n++)
         for (int l = 1 - NGC; l <= p->lf + NGC; l++) {
             double vx, vy, vx2, vy2, pres, c;
             c2p_local(UP(U, G, l, n), &vx, &vy, &vx2, &vy2, &pres, &c, NULL);
-            dt = fmin(dt, 1.0 / (1.0 / (dx / (fabs(vx) + c)) + 1.0 / (dy / (fabs(vy) + c))));
+            if (p->setdt_kind == 1) /* deprecated/physics.f90:106-118 */
+                dt = fmin(dt, fmin(dx0 / (fabs(vx) + c), dy0 / (fabs(vy) + c)));
+            else
+                dt = fmin(dt, 1.0 / (1.0 / (dx / (fabs(vx) + c)) + 1.0 / (dy / (fabs(vy) + c))));
         }
+    if (reduce) dt = dt * pow(dx / dx0, (double)p->mord / 4); /* deprecated/physics.f90:122-124 */
     dt = dt * p->cfl;
     if (dt > dtfinal) dt = dtfinal;
     return dt;
@@ -686,6 +693,8 @@ struct orc_ctx {
     double *rk4[5];  /* U3, U4, FU3, FU4, Fl of SSP_RK4_ (U1, U2 are u1, u2), on first use */
     int cc_col;      /* NN_GP_MOOD_CC_ blend column (the input count L), or -1 */
     float *cc_w;     /* values_NN(cc_col, n, 1:2) for n = 0..nf+1; NULL: no blend */
+    double dt_sim;   /* deprecated/main.f90 slow-start step (0: off) */
+    int pol_fd;      /* POL_MOOD: U2 from D2O2 finite differences (mod_subroutine_MOOD.f90:81-84) */
 };
 
 /* NN_GP_MOOD_CC_ (mod_NN_GP_MOOD_CC.f90:11-85): with w != NULL every face
@@ -712,6 +721,7 @@ orc_ctx* orc_create(const orc_params* p)
     orc_ctx* c = (orc_ctx*)calloc(1, sizeof *c);
     if (!c) return NULL;
     c->p = *p;
+    c->dt_sim = p->slow_start > 0 ? fmin(p->slow_start, 1e30) : 0; /* dt_sim = min(1.e-10, dt), dt = 1e30 */
     if (orc_gp_presim(p, &c->gp) != 0) { free(c); return NULL; }
     if (p->method == 200 || p->method == 201) {
         /* POL_MOOD_ / Unlim_POL_ (mod_pol_MOOD.f90, mod_Unlim_Pol.f90): the
@@ -730,6 +740,7 @@ orc_ctx* orc_create(const orc_params* p)
                 for (int m = 0; m < 5; m++) c->gp.zt[1][f][j][m] = oc[tab[f][j][m]];
                 c->gp.zt[0][f][j][0] = 1.0;
             }
+        c->pol_fd = p->method == 200;
         c->p.method = p->method == 200 ? 2 : 202;
     }
     if (p->method == 1) { /* FOG_ (mod_FOG.f90): Uh = Uin, no DETECTION: GP_SE at order 1 */
@@ -887,6 +898,18 @@ static long long detection(orc_ctx* c, const double* Uin, double* Uout, double t
                                         for (int j = -1; j <= 1; j++)
                                             for (int i = -1; i <= 1; i++) {
                                                 if (!(i == 0 || j == 0)) continue;
+                                                if (c->pol_fd) { /* POL_MOOD, :81-84: D2O2 = (1,-2,1), /dx**2 */
+                                                    const double m = UP(Uin, G, l + i, n + j)[RHO];
+                                                    double sx = 0.0 + 1. * UP(Uin, G, l + i - 1, n + j)[RHO];
+                                                    sx = sx + (-2.) * m;
+                                                    sx = sx + 1. * UP(Uin, G, l + i + 1, n + j)[RHO];
+                                                    double sy = 0.0 + 1. * UP(Uin, G, l + i, n + j - 1)[RHO];
+                                                    sy = sy + (-2.) * m;
+                                                    sy = sy + 1. * UP(Uin, G, l + i, n + j + 1)[RHO];
+                                                    D2x[i + 1][j + 1] = sx / (dx * dx);
+                                                    D2y[i + 1][j + 1] = sy / (dy * dy);
+                                                    continue;
+                                                }
                                                 double q[5];
                                                 for (int k = 0; k < 5; k++)
                                                     q[k] = UP(Uin, G, l + k_ixiy[k][0] + i, n + k_ixiy[k][1] + j)[RHO];
@@ -965,6 +988,8 @@ int orc_shock_detector(const orc_params* p, const double* Uin, int l, int n) /* 
     Mach = sqrt(Mach / Ca);
     double pL = orc_pressure(ul), pR = orc_pressure(ur), pB = orc_pressure(ub), pT = orc_pressure(ut);
     double gradP = 0.5 * (fabs(pR - pL) / fmin(pL, pR) / dx + fabs(pT - pB) / fmin(pB, pT) / dy);
+    if (p->csd_kind == 1) return (divV < -threshold1) && (gradP > threshold1); /* threshold2 = threshold1 */
+    if (p->csd_kind == 2) return 1;
     double mxd = fmax(dx, dy);
     return (divV < -(mxd * mxd)) && (Mach > 0.2) && (gradP > threshold1);
 }
@@ -1210,6 +1235,10 @@ int orc_run(orc_ctx* c, double* U, double* t_io, int nsteps, long long* counters
         niter++;
         double dtfinal = c->p.tmax - t;
         double dt = orc_setdt(&c->p, U, dtfinal);
+        if (c->dt_sim > 0 && c->dt_sim < dt) { /* deprecated/main.f90: force a small dt for a slow start */
+            dt = c->dt_sim;
+            c->dt_sim = 2. * c->dt_sim;
+        }
         int rc = orc_time_stepping(c, U, Ur, t, dt, NULL, NULL, counters);
         if (rc) { free(Ur); return rc; }
         t = t + dt;

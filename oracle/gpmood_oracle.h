@@ -5,15 +5,18 @@
  * tests/, __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm
  * may load it.  The product library (libgpmood) never links or calls it.
  *
- * Parity status: the reference is Fortran and no Fortran compiler exists on
- * either machine, so the reference itself cannot be run.  The restatement is
- * pinned by (i) the reference's own GP inversion self-check
- * (gp-mood-code/GP_init.f90:250), (ii) an independent arbitrary-precision
- * (mpmath) recomputation of every GP weight, (iii) the x<->y diagonal symmetry
- * metric of gp-mood-code/plot/plotter_hdf5.py:43 and (iv) the recorded
- * isentropic-vortex L1 convergence data of the deprecated code line
- * (deprecated/plotter_revision/Isentropic/).  Against the Fortran binary
- * itself parity is unpinned.
+ * Parity status: pinned to the reference's own recorded outputs.  No
+ * Fortran compiler exists on either machine, but the reference's deprecated
+ * code line recorded final states of real runs
+ * (deprecated/plotter_revision/{2DRP_C3,Isentropic}/).  With that line's
+ * Setdt and slow start (the setdt_kind / slow_start knobs below; its solver
+ * step is gp-mood-code's), the restatement reproduces the 2DRP3 runs at 200^2
+ * and 400^2 -- R1 and R2 GP, POL_MOOD, SSP-RK3 and SSP-RK4, 487 to 1037 steps
+ * with MOOD active -- bit for bit with the same step counts, and the
+ * isentropic-vortex runs from their recorded initial states to 1e-15
+ * relative L1 (tests/test_reference_pins.py).  Further checks: the
+ * reference's GP inversion self-check (gp-mood-code/GP_init.f90:250) and an
+ * independent arbitrary-precision (mpmath) recomputation of every GP weight.
  *
  * Layout follows the reference: U(4, lb:le, nb:ne), variable fastest
  * (gp-mood-code/global_variables.f90:26), lb = 1-ngc, le = lf+ngc, ngc = 4.
@@ -41,6 +44,19 @@ typedef struct orc_params {
     int bc_type;       /* 17 Neumann, 18 Periodic, 20 Reflective, 35 DMR */
     int integrator;    /* 8 FE, 9 SSP_RK2, 10 SSP_RK3 (default for 0), 12 SSP_RK4 (constants.f90:19) */
     int num_flux;      /* 100 HLLC (default for 0), 101 LLF, 102 HLL, 103 unsplit (constants.f90:21) */
+    /* Knobs of the deprecated code line, which recorded the reference's only
+     * per-cell output snapshots (deprecated/plotter_revision/Isentropic/);
+     * all zero = gp-mood-code's behaviour. */
+    int setdt_kind;    /* 0: physics.f90:110, dt = min 1/(1/(dx/(|u|+c)) + 1/(dy/(|v|+c)));
+                          1: deprecated/physics.f90:106-118, dt = min(dx/(|u|+c), dy/(|v|+c)) */
+    int lf0, nf0;      /* deprecated dt_reduction base grid (deprecated/physics.f90:94-126); 0 = off */
+    double slow_start; /* deprecated/main.f90 slow start: the first steps take dt_sim, which starts
+                          at min(slow_start, 1e30) and doubles each step while it is below the CFL dt;
+                          0 = off */
+    int csd_kind;      /* shock detector gating the DMP test: 0 mod_subroutine_MOOD.f90:231
+                          (divV < -max(dx,dy)^2, Mach > 0.2, gradP > 5); 1 the deprecated line's
+                          "old CSD" (deprecated/mod_subroutine_MOOD.f90:104, divV < -5, gradP > 5);
+                          2 none (the DMP test on every checked cell, the "noCSD" runs) */
 } orc_params;
 
 /* GP weights as produced by GP_presim_sphere (GP_init.f90:26-357).

@@ -2,8 +2,8 @@
 
 TEST INFRASTRUCTURE ONLY: the checker for the CUDA path.  Only tests/,
 __graft_entry__.smoke() and bench.py's CPU-baseline / reference arm load it.
-Parity against the Fortran reference binary is unpinned (no Fortran compiler
-exists here or on the GPU host); gpmood_oracle.h lists the checks that pin it.
+Pinned to the reference's own recorded runs (bit for bit on the deprecated
+code line's 2DRP3 outputs; gpmood_oracle.h lists the pins).
 """
 from __future__ import annotations
 
@@ -31,7 +31,8 @@ class OrcParams(C.Structure):
     _fields_ = [("cfl", C.c_double), ("ell_o_dx", C.c_double), ("lx", C.c_double), ("ly", C.c_double),
                 ("tmax", C.c_double), ("mord", C.c_int), ("ngp", C.c_int), ("method", C.c_int),
                 ("dmp", C.c_int), ("u2", C.c_int), ("u2_tol", C.c_int), ("lf", C.c_int), ("nf", C.c_int),
-                ("bc_type", C.c_int), ("integrator", C.c_int), ("num_flux", C.c_int)]
+                ("bc_type", C.c_int), ("integrator", C.c_int), ("num_flux", C.c_int), ("setdt_kind", C.c_int),
+                ("lf0", C.c_int), ("nf0", C.c_int), ("slow_start", C.c_double), ("csd_kind", C.c_int)]
 
 
 class OrcGp(C.Structure):
@@ -92,9 +93,13 @@ def lib() -> C.CDLL:
 
 
 def make_params(lf, nf, *, lx=1.0, ly=1.0, tmax=0.8, mord=5, ngp=3, method=GP_MOOD, bc=NEUMANN, cfl=0.8,
-                ell_o_dx=12.0, dmp=1, u2=1, u2_tol=1, integrator=SSP_RK3, num_flux=HLLC) -> OrcParams:
+                ell_o_dx=12.0, dmp=1, u2=1, u2_tol=1, integrator=SSP_RK3, num_flux=HLLC, setdt_kind=0, lf0=0,
+                nf0=0, slow_start=0.0, csd_kind=0) -> OrcParams:
+    """The knobs of parameters.f90; setdt_kind, lf0/nf0, slow_start and csd_kind
+    select the deprecated code line's time step and shock detector (see
+    gpmood_oracle.h)."""
     return OrcParams(cfl, ell_o_dx, lx, ly, tmax, mord, ngp, method, dmp, u2, u2_tol, lf, nf, bc, integrator,
-                     num_flux)
+                     num_flux, setdt_kind, lf0, nf0, slow_start, csd_kind)
 
 
 def padded(lf: int, nf: int) -> np.ndarray:

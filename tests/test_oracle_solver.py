@@ -1,5 +1,6 @@
-"""Invariants of the CPU oracle's solver: the reference's own checks and the
-published (deprecated-code) numbers that pin the restatement."""
+"""Invariants of the CPU oracle's solver and the reference's GP inversion
+self-check; the reference's recorded runs are reproduced in
+tests/test_reference_pins.py."""
 from __future__ import annotations
 
 import numpy as np
@@ -79,20 +80,6 @@ def test_shock_detector_cases(oracle):
     # the same jump in a diverging flow is not a shock
     U[..., 1] = -U[..., 1]
     assert oracle.lib().orc_shock_detector(C.byref(p), U, 8, 8) == 0
-
-
-@pytest.mark.parametrize("n,ref,rel", [(50, 1.1374606777349294, 0.05), (100, 0.16745924640337226, 0.05)])
-def test_deprecated_vortex_l1_anchor(oracle, n, ref, rel):
-    """deprecated/plotter_revision/Isentropic/isen_GP3rd_2quad_RK3_cfl0.8_HLLC_Lx20_*_ell_1.0_sphere_error_L1.dat:
-    GP3 (R1, 2 Gauss points), SSP-RK3, HLLC, CFL 0.8, ell = 1 (absolute), Lx = 20,
-    one period (tmax = 20).  The deprecated code differs in details; a loose anchor."""
-    dx = 20.0 / n
-    p = oracle.make_params(n, n, lx=20.0, ly=20.0, tmax=20.0, mord=3, ngp=2, bc=18, ell_o_dx=1.0 / dx)
-    U0 = oracle.initial_condition(p, "vortex")
-    U, t, k, _ = run(oracle, p, "vortex", 10 ** 7)
-    assert t == 20.0
-    err = np.abs(U0[I + (0,)] - U[I + (0,)]).sum() * dx * dx
-    assert abs(err - ref) < rel * ref, (err, ref)
 
 
 @pytest.mark.parametrize("n,ref", [(50, 1.8488927466117464E-032), (100, 3.9443045261050590E-031),
