@@ -18,7 +18,6 @@ from __future__ import annotations
 import argparse
 import json
 import os
-import re
 import statistics
 import subprocess
 import sys
@@ -170,14 +169,11 @@ def measured_peaks():
         return None
 
 
-def ncu_traffic_per_face():
-    """DRAM bytes per face of the fast first-pass face kernel from the committed ncu summary."""
-    f = ROOT / "profiles" / "ncu_flux_sedov2048.md"
-    try:
-        m = re.search(r"dram_bytes_per_face:\s*([0-9.eE+-]+)", f.read_text())
-        return float(m.group(1)) if m else None
-    except OSError:
-        return None
+# DRAM bytes per face of one launch of the fast two-direction face kernel
+# (k_flux_xy) on the 2048^2 Sedov first pass, from one ncu capture of this
+# workload: dram__bytes_read.sum + dram__bytes_write.sum = 135.91 MB + 219.94 MB
+# over 8,392,704 faces.  A constant of that capture, not a live measurement.
+DRAM_BYTES_PER_FACE_NCU = 42.40
 
 
 def cpu_oracle_rate(n, steps, threads):
@@ -534,7 +530,7 @@ def run_ours(args, ws, rank, local):
     faces_per_launch = tm.flux_faces / max(tm.flux_launches, 1)
     achieved_tflops = FLOPS_PER_FACE * faces_per_launch / (launch_ms * 1e-3) / 1e12
     peak_tflops = peak_fp64_gflops / 1e3
-    tpf = ncu_traffic_per_face() if fp == pkg.FP_FAST else None  # the committed capture is of the fast kernel
+    tpf = DRAM_BYTES_PER_FACE_NCU if fp == pkg.FP_FAST else None  # the capture is of the fast kernel
     kname = ("first pass of one RK stage: k_flux_xy (interior, both directions) + k_flux_edge (faces of ghost "
              "cells); GP recon + HLLC + quadrature" if fp == pkg.FP_FAST
              else "first pass of one RK stage: k_flux_tile x and y (GP recon + HLLC + quadrature)")
