@@ -13,6 +13,17 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <atomic>
+
+// Kernel attributes and occupancy-derived grid sizes belong to a device, so
+// the launchers keep them per device index (at most GPM_MAX_DEVICES).
+#define GPM_MAX_DEVICES 64
+inline int gpm_device() {
+    int d = 0;
+    cudaGetDevice(&d);
+    return d >= 0 && d < GPM_MAX_DEVICES ? d : 0;
+}
+
 #define GPM_NGC 4
 #define GPM_MAXGP 5
 #define GPM_MAXST 5  // RK stages of the longest integrator (SSP-RK4: 5 Forward_Euler calls)

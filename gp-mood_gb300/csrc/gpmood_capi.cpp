@@ -410,6 +410,8 @@ void free_all(gpmood_ctx* c) {
 
 void gpm_set_thread_error(const char* msg) { snprintf(g_err, sizeof g_err, "%s", msg); }
 
+int gpm_validate_params(const gpmood_params* p, char* why, size_t n) { return validate(p, why, n); }
+
 extern "C" {
 
 int gpmood_default_params(gpmood_params* p) {

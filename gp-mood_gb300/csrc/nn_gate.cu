@@ -718,13 +718,14 @@ int nn_gate_orders(NnGate* n, const GridGeom& g, const double* uin, int8_t* orde
     if (!n->loaded || g.mord < 3) return 0;
     const long long cells = (long long)g.lf * g.nf;
     const long long tiles = (cells + TC_THREADS - 1) / TC_THREADS;
-    static int nsm = 0;
+    static std::atomic<int> nsms[GPM_MAX_DEVICES];
+    const int dev = gpm_device();
+    int nsm = nsms[dev].load(std::memory_order_relaxed);
     if (!nsm) {
-        int dev = 0;
-        cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
         if (nsm <= 0) nsm = 1;
         cudaFuncSetAttribute(k_gate, cudaFuncAttributeMaxDynamicSharedMemorySize, TC_SMEM);
+        nsms[dev].store(nsm, std::memory_order_relaxed);
     }
     // persistent: 4 CTAs per SM, each holding 128 of the SM's 512 TMEM columns
     const int blocks = (int)(tiles < 4LL * nsm ? tiles : 4LL * nsm);
@@ -750,10 +751,11 @@ static int train_launch(const float* p, const float* x, const float* y, int n, f
                         int fwd_only, float* logits, cudaStream_t s) {
     if (n <= 0) return -1;
     const size_t sm = sizeof(SmemTrain);
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<bool> attr[GPM_MAX_DEVICES];
+    const int dev = gpm_device();
+    if (!attr[dev].load(std::memory_order_relaxed)) {
         cudaFuncSetAttribute(k_train, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sm);
-        attr = true;
+        attr[dev].store(true, std::memory_order_relaxed);
     }
     k_train<<<(n + ROWS - 1) / ROWS, THREADS, sm, s>>>(p, x, y, n, pw, 1.0f / (float)n, grad, loss, fwd_only, logits);
     return cudaGetLastError() == cudaSuccess ? 0 : -1;

@@ -492,10 +492,11 @@ __global__ void __launch_bounds__(EDGE_T) k_flux_edge(StageArgs a, const __grid_
 }
 
 bool launch_flux_xy(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
-    static bool attr = false;
-    if (!attr) {
+    static std::atomic<bool> attr[GPM_MAX_DEVICES];
+    const int dev = gpm_device();
+    if (!attr[dev].load(std::memory_order_relaxed)) {
         cudaFuncSetAttribute(k_flux_xy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(XySmem));
-        attr = true;
+        attr[dev].store(true, std::memory_order_relaxed);
     }
     const int tx = (a.g.lf + XT - 1) / XT, ty = (a.g.nf + XY - 1) / XY;
     const int edges = (a.g.lf + a.g.nf + EDGE_T - 1) / EDGE_T;
@@ -948,13 +949,15 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
 template <int NGP>
 static int launch_mood_loop_n(const StageArgs& a, const GpWeights& w, GridBar* bar, int max_pass, int stage,
                               cudaStream_t s) {
-    static int grid = 0;
+    static std::atomic<int> grids[GPM_MAX_DEVICES];
+    const int dev = gpm_device();
+    int grid = grids[dev].load(std::memory_order_relaxed);
     if (!grid) {
-        int dev = 0, sms = 0, occ = 0;
-        cudaGetDevice(&dev);
+        int sms = 0, occ = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mood_loop<NGP>, MOOD_THREADS, 0);
         grid = sms * (occ > 0 ? occ : 1);
+        grids[dev].store(grid, std::memory_order_relaxed);
     }
     StageArgs aa = a;
     GpWeights ww = w;
@@ -1298,14 +1301,16 @@ __global__ void __launch_bounds__(EDGE_T) kb_flux_edge(BatchArgs a) {
 }
 #endif
 
-static int g_sms = 0;
 static int sm_count() {
-    if (!g_sms) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&g_sms, cudaDevAttrMultiProcessorCount, dev);
+    static std::atomic<int> sms[GPM_MAX_DEVICES];
+    const int dev = gpm_device();
+    int n = sms[dev].load(std::memory_order_relaxed);
+    if (!n) {
+        cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
+        if (n <= 0) n = 1;
+        sms[dev].store(n, std::memory_order_relaxed);
     }
-    return g_sms;
+    return n;
 }
 
 template <int TXB, int TYB, int NGP>
@@ -1321,10 +1326,11 @@ template <int NGP>
 static void blaunch_flux_n(const BatchArgs& a, cudaStream_t s) {
 #if !GPM_EXACT
     if (a.tile == GPM_TILE_XY && NGP == 3 && a.mord == 5) {
-        static bool attr = false;
-        if (!attr) {
+        static std::atomic<bool> attr[GPM_MAX_DEVICES];
+        const int dev = gpm_device();
+        if (!attr[dev].load(std::memory_order_relaxed)) {
             cudaFuncSetAttribute(kb_flux_xy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(XySmem));
-            attr = true;
+            attr[dev].store(true, std::memory_order_relaxed);
         }
         const int grid = a.nftiles < sm_count() * 2 ? a.nftiles : sm_count() * 2;
         kb_flux_xy<<<grid, dim3(XT, XY), sizeof(XySmem), s>>>(a);
@@ -1553,11 +1559,14 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) kb_mood_loop(BatchArgs a, Gri
 
 template <int NGP>
 static int blaunch_mood_loop_n(const BatchArgs& a, GridBar* bar, int max_pass, cudaStream_t s) {
-    static int grid = 0;
+    static std::atomic<int> grids[GPM_MAX_DEVICES];
+    const int dev = gpm_device();
+    int grid = grids[dev].load(std::memory_order_relaxed);
     if (!grid) {
         int occ = 0;
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kb_mood_loop<NGP>, MOOD_THREADS, 0);
         grid = sm_count() * (occ > 0 ? occ : 1);
+        grids[dev].store(grid, std::memory_order_relaxed);
     }
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(grid);

@@ -101,7 +101,7 @@ SIGNATURES = {
     "gpmood_probe_fp64": ([_DP], C.c_int),
     "gpmood_fast_rcp": ([C.c_void_p, C.c_void_p, C.c_int], C.c_int),
     "gpmood_time_stepping_noalloc": ([C.POINTER(Params), C.c_void_p, C.c_void_p, C.c_double, C.c_double,
-                                      C.c_void_p], C.c_int),
+                                      C.c_void_p, C.POINTER(C.c_int)], C.c_int),
     "gpmood_batch_create": ([C.POINTER(Params), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
                              C.POINTER(C.c_void_p)], C.c_int),
     "gpmood_batch_destroy": ([C.c_void_p], None),

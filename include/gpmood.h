@@ -204,13 +204,19 @@ int  gpmood_time_stepping_dev(gpmood_ctx* ctx, double* d_uin, double* d_uout,
  * d_uout are the caller's device arrays in the padded layout; every scratch
  * array lives in a static device buffer of ~10 MB that every GPU loading the
  * library holds until exit, so grids are limited to (lf+8)*(nf+8) <= 264*264
- * (GPMOOD_E_ARG beyond that).  method GP_MOOD or GP_SE.  The first call on a
- * device looks up that buffer's address, so make it before any stream
+ * (GPMOOD_E_ARG beyond that).  The knobs are checked as gpmood_create checks
+ * them; method GP_MOOD or GP_SE, SSP-RK3, Neumann, periodic, reflective or
+ * DMR boundaries.  The first call on a device (and in each new CUDA context
+ * on it) looks up that buffer's address, so make it before any stream
  * capture.  All calls share the buffer: calls that overlap on the GPU race.
  * stream is a cudaStream_t (NULL = legacy default stream); the call is
- * synchronous at return.  Errors: gpmood_last_error(NULL, ...). */
+ * synchronous at return.  *status (may be NULL) receives the step's status
+ * bits, those of gpmood_counters.status_flags: bit 0 (a NaN or inadmissible
+ * state left in an order-1 cell) leaves the call successful, as in the
+ * reference; a MOOD cap (bit 1) returns GPMOOD_E_MOOD_CAP after the whole step
+ * ran, as gpmood_time_stepping does.  Errors: gpmood_last_error(NULL, ...). */
 int  gpmood_time_stepping_noalloc(const gpmood_params* p, double* d_uin, double* d_uout,
-                                  double t, double dt, void* stream);
+                                  double t, double dt, void* stream, int* status);
 
 /* ---- many independent problems of uneven size (one GPU) ---- */
 
