@@ -170,10 +170,10 @@ def measured_peaks():
 
 
 # DRAM bytes per face of one launch of the fast two-direction face kernel
-# (k_flux_xy) on the 2048^2 Sedov first pass, from one ncu capture of this
-# workload: dram__bytes_read.sum + dram__bytes_write.sum = 135.91 MB + 219.94 MB
+# (k_flux_xy_tma) on the 2048^2 Sedov first pass, from one ncu capture of this
+# workload: dram__bytes_read.sum + dram__bytes_write.sum = 136.27 MB + 208.18 MB
 # over 8,392,704 faces.  A constant of that capture, not a live measurement.
-DRAM_BYTES_PER_FACE_NCU = 42.40
+DRAM_BYTES_PER_FACE_NCU = 41.04
 
 
 def cpu_oracle_rate(n, steps, threads):
@@ -525,14 +525,14 @@ def run_ours(args, ws, rank, local):
 
     # ---- roofline of the dominant kernel (first-pass face kernel) ----
     # one "launch" of the roofline = the first pass of one RK stage: every face
-    # of the grid (fast mode: k_flux_xy + k_flux_edge; exact: the x and y kernels)
+    # of the grid (fast mode: k_flux_xy_tma + k_flux_edge; exact: the x and y kernels)
     launch_ms = tm.flux_ms / max(tm.flux_launches, 1)
     faces_per_launch = tm.flux_faces / max(tm.flux_launches, 1)
     achieved_tflops = FLOPS_PER_FACE * faces_per_launch / (launch_ms * 1e-3) / 1e12
     peak_tflops = peak_fp64_gflops / 1e3
     tpf = DRAM_BYTES_PER_FACE_NCU if fp == pkg.FP_FAST else None  # the capture is of the fast kernel
-    kname = ("first pass of one RK stage: k_flux_xy (interior, both directions) + k_flux_edge (faces of ghost "
-             "cells); GP recon + HLLC + quadrature" if fp == pkg.FP_FAST
+    kname = ("first pass of one RK stage: k_flux_xy_tma (interior, both directions, TMA-staged halo tiles) + "
+             "k_flux_edge (faces of ghost cells); GP recon + HLLC + quadrature" if fp == pkg.FP_FAST
              else "first pass of one RK stage: k_flux_tile x and y (GP recon + HLLC + quadrature)")
     roofline = {"bound": "fp64", "kernel": kname,
                 "achieved": achieved_tflops, "peak": peak_tflops, "unit": "TFLOP/s",

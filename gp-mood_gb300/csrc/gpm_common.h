@@ -87,12 +87,18 @@ struct GridGeom {
                          // D2O2/dx^2 (mod_subroutine_MOOD.f90:81-84) instead of the GP weights
     int num_flux;        // 100 HLLC, 101 LLF, 102 HLL, 103 unsplit
     int mood_solo;       // device MOOD loop: lists of at most this many cells run in one CTA
+    int flux_tma;        // fast first pass: halo tiles staged by a TMA bulk tensor copy (1) or loads (0)
     int cc_col;          // NN_GP_MOOD_CC: the column l whose order-3 states are blended (-1: none)
 };
 
 // Default of GridGeom::mood_solo; the environment variable GPMOOD_MOOD_SOLO
 // overrides it (tuning only: results do not depend on it).
 int gpm_mood_solo_default();
+
+// Default of GridGeom::flux_tma (1); the environment variable GPMOOD_FLUX_TMA=0
+// selects the plain-load staging (A/B timing only: the staged tile, and so
+// every result, is the same either way).  Read at context creation.
+int gpm_flux_tma_default();
 
 // Scalars that stay on the device across a step.
 struct DevScalars {
@@ -109,7 +115,8 @@ struct DevScalars {
 };
 
 enum { GPM_STATUS_NAN = 1, GPM_STATUS_MOODCAP = 2, GPM_STATUS_DT = 4, GPM_STATUS_BARRIER = 8,
-       GPM_STATUS_TENSOR = 16 };  // a tensor-core (tcgen05) wait timed out
+       GPM_STATUS_TENSOR = 16,  // a tensor-core (tcgen05) wait timed out
+       GPM_STATUS_TMA = 32 };   // a TMA tile copy's mbarrier wait timed out
 
 // Grid barrier state of the cooperative MOOD-loop kernel (zeroed device memory).
 struct GridBar {

@@ -73,6 +73,11 @@ int gpm_mood_solo_default() {
     return v;
 }
 
+int gpm_flux_tma_default() {
+    const char* e = getenv("GPMOOD_FLUX_TMA");
+    return e && *e ? (atoi(e) != 0) : 1;
+}
+
 namespace {
 
 // NVTX range over a host scope (steps and stages show up on an Nsight Systems
@@ -474,6 +479,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     c->g.method = c->p.method;
     c->g.num_flux = p->num_flux;
     c->g.mood_solo = gpm_mood_solo_default();
+    c->g.flux_tma = gpm_flux_tma_default();
     c->g.cc_col = -1;
     c->nstages = p->integrator == GPMOOD_FE ? 1 : p->integrator == GPMOOD_SSP_RK2 ? 2 : p->integrator == GPMOOD_SSP_RK4 ? 5 : 3;
     c->g.dmp = p->dmp;

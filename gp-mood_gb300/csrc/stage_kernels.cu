@@ -31,6 +31,11 @@
 // accumulation order, reproduces the reference bit for bit.
 #include "physics.cuh"
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
+
+#include <mutex>
+
 #if GPM_EXACT
 #define GPM_NS gpm_exact
 #else
@@ -391,15 +396,18 @@ struct XySmem {
     double bottom[XY][XT][XS];  // bottom-face states of rows n0+1 .. n0+XY
 };
 
+// staged: the halo tile is already in sm.tile (TMA); otherwise load it here.
 __device__ __forceinline__ void xy_tile(const GridGeom& g, const GpWeights& w, const double* __restrict__ uin,
                                         double* __restrict__ fx, double* __restrict__ fy, int l0, int n0,
-                                        XySmem& sm) {
+                                        XySmem& sm, bool staged) {
     const int tx = threadIdx.x, ty = threadIdx.y, tid = ty * XT + tx;
-    for (int i = tid; i < (XT + 5) * (XY + 5); i += XT * XY) {
-        const int cy = i / (XT + 5), cx = i - cy * (XT + 5);
-        const int l = l0 - 2 + cx, n = n0 - 2 + cy;
-        if (l >= -3 && l <= g.lf + 4 && n >= -3 && n <= g.nf + 4) sm.tile[cy][cx] = ld_cell(uin + 4 * cidx(g, l, n));
-    }
+    if (!staged)
+        for (int i = tid; i < (XT + 5) * (XY + 5); i += XT * XY) {
+            const int cy = i / (XT + 5), cx = i - cy * (XT + 5);
+            const int l = l0 - 2 + cx, n = n0 - 2 + cy;
+            if (l >= -3 && l <= g.lf + 4 && n >= -3 && n <= g.nf + 4)
+                sm.tile[cy][cx] = ld_cell(uin + 4 * cidx(g, l, n));
+        }
     __syncthreads();
     const int l = l0 + tx, n = n0 + ty;
     // a cell up to (lf+1, nf+1) provides states: its stencil stays inside the padded grid
@@ -483,7 +491,98 @@ __global__ void __launch_bounds__(XT * XY) k_flux_xy(StageArgs a, const __grid_c
     extern __shared__ __align__(16) unsigned char xy_raw[];
     XySmem& sm = *reinterpret_cast<XySmem*>(xy_raw);
     const int by = blockIdx.x / tiles_x, bx = blockIdx.x - by * tiles_x;
-    xy_tile(a.g, w, a.uin, a.fx, a.fy, 1 + bx * XT, 1 + by * XY, sm);
+    xy_tile(a.g, w, a.uin, a.fx, a.fy, 1 + bx * XT, 1 + by * XY, sm, false);
+}
+
+// ---- the same kernel with the halo tile staged by the Tensor Memory Accelerator
+// The padded state is a 2-D tensor of ny rows by 4*nx doubles; one
+// cp.async.bulk.tensor copies the tile's (XY+5) rows of 4*(XT+5) doubles --
+// exactly the row-major layout of XySmem::tile -- into this CTA's own shared
+// memory and completes on an mbarrier.  The innermost start coordinate is
+// 4*(l0+1) doubles, a multiple of 32 bytes; boxes that reach past the padded
+// grid on the right or top are zero-filled, and those cells feed no live
+// cell's stencil.
+constexpr unsigned XY_TILE_BYTES = (unsigned)sizeof(Cell) * (XT + 5) * (XY + 5);
+static_assert(sizeof(XySmem::tile) == XY_TILE_BYTES, "TMA box = staged tile");
+static_assert(sizeof(XySmem) % 8 == 0, "mbarrier after the tile data");
+
+__device__ __forceinline__ uint32_t smem_addr(const void* p) { return (uint32_t)__cvta_generic_to_shared(p); }
+
+// Bounded wait for phase `parity` of an mbarrier (~1 s at most).
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t parity) {
+    for (int it = 0; it < (1 << 20); it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_addr(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    return false;
+}
+
+__global__ void __launch_bounds__(XT * XY) k_flux_xy_tma(StageArgs a, const __grid_constant__ GpWeights w,
+                                                         const __grid_constant__ CUtensorMap tm, int tiles_x) {
+    extern __shared__ __align__(1024) unsigned char xy_raw[];
+    XySmem& sm = *reinterpret_cast<XySmem*>(xy_raw);
+    unsigned long long* bar = reinterpret_cast<unsigned long long*>(xy_raw + sizeof(XySmem));
+    const int by = blockIdx.x / tiles_x, bx = blockIdx.x - by * tiles_x;
+    const int l0 = 1 + bx * XT, n0 = 1 + by * XY;
+    if (threadIdx.x == 0 && threadIdx.y == 0) {
+        asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(smem_addr(bar)) : "memory");
+        asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_addr(bar)),
+                     "r"(XY_TILE_BYTES)
+                     : "memory");
+        // padded cell (l0-2, n0-2) is column l0+1, row n0+1 of the padded grid
+        asm volatile(
+            "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], "
+            "[%4];" ::"r"(smem_addr(&sm.tile[0][0])),
+            "l"(reinterpret_cast<uint64_t>(&tm)), "r"(4 * (l0 + 1)), "r"(n0 + 1), "r"(smem_addr(bar))
+            : "memory");
+    }
+    __syncthreads();  // the barrier is initialised before anyone waits on it
+    const bool ok = mbar_wait(bar, 0);
+    if (!__syncthreads_and(ok)) {
+        if (threadIdx.x == 0 && threadIdx.y == 0) {
+            atomicOr(&a.sc->status, GPM_STATUS_TMA);
+            mbar_wait(bar, 0);  // once more, bounded, for the copy in flight before the CTA leaves
+        }
+        return;
+    }
+    xy_tile(a.g, w, a.uin, a.fx, a.fy, l0, n0, sm, true);
+}
+
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no -lcuda).
+static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+    static std::once_flag once;
+    std::call_once(once, [] {
+        void* f = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &f, 12000, cudaEnableDefault, &q) ==
+                cudaSuccess &&
+            q == cudaDriverEntryPointSuccess)
+            fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(f);
+    });
+    return fn;
+}
+
+// The tile map of a padded state: ny rows of 4*nx doubles, boxes of XY+5 rows
+// by 4*(XT+5) doubles.  False if the driver refuses it or the state is not
+// 16-byte aligned (TMA's rule for the global address).
+static bool encode_tile_map(CUtensorMap* m, const double* u, const GridGeom& g) {
+    PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
+    if (!enc || (reinterpret_cast<uintptr_t>(u) & 15)) return false;
+    const cuuint64_t dims[2] = {(cuuint64_t)4 * g.nx, (cuuint64_t)g.ny};
+    const cuuint64_t strides[1] = {(cuuint64_t)4 * g.nx * sizeof(double)};
+    const cuuint32_t box[2] = {4 * (XT + 5), XY + 5};
+    const cuuint32_t estr[2] = {1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT64, 2, const_cast<double*>(u), dims, strides, box, estr,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
 // The faces whose low cell is a ghost, EDGE_T per block.
@@ -494,13 +593,19 @@ __global__ void __launch_bounds__(EDGE_T) k_flux_edge(StageArgs a, const __grid_
 bool launch_flux_xy(const StageArgs& a, const GpWeights& w, cudaStream_t s) {
     static std::atomic<bool> attr[GPM_MAX_DEVICES];
     const int dev = gpm_device();
+    constexpr int tma_smem = (int)sizeof(XySmem) + 8;  // + the mbarrier
     if (!attr[dev].load(std::memory_order_relaxed)) {
         cudaFuncSetAttribute(k_flux_xy, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(XySmem));
+        cudaFuncSetAttribute(k_flux_xy_tma, cudaFuncAttributeMaxDynamicSharedMemorySize, tma_smem);
         attr[dev].store(true, std::memory_order_relaxed);
     }
     const int tx = (a.g.lf + XT - 1) / XT, ty = (a.g.nf + XY - 1) / XY;
     const int edges = (a.g.lf + a.g.nf + EDGE_T - 1) / EDGE_T;
-    k_flux_xy<<<tx * ty, dim3(XT, XY), sizeof(XySmem), s>>>(a, w, tx);
+    CUtensorMap tm;
+    if (a.g.flux_tma && encode_tile_map(&tm, a.uin, a.g))
+        k_flux_xy_tma<<<tx * ty, dim3(XT, XY), tma_smem, s>>>(a, w, tm, tx);
+    else
+        k_flux_xy<<<tx * ty, dim3(XT, XY), sizeof(XySmem), s>>>(a, w, tx);
     k_flux_edge<<<edges, EDGE_T, 0, s>>>(a, w);
     return true;
 }
@@ -1169,6 +1274,7 @@ __device__ __forceinline__ GridGeom bgeom(const BatchArgs& a, const BProb& p) {
     g.bc_type = a.bc_type; g.ngp = a.ngp; g.mord = a.mord; g.method = a.method;
     g.dmp = a.dmp; g.u2 = a.u2; g.u2_tol = a.u2_tol; g.u2_fd = 0; g.num_flux = a.num_flux;
     g.mood_solo = a.mood_solo;
+    g.flux_tma = 0;
     g.cc_col = -1;
     return g;
 }
@@ -1287,7 +1393,7 @@ __global__ void __launch_bounds__(XT * XY, 2) kb_flux_xy(BatchArgs a) {
         const int4 it = a.ftiles[item];
         const BProb P = a.prob[it.x];
         __syncthreads();  // the previous tile is done with the shared buffers
-        xy_tile(bgeom(a, P), a.wtab[P.wc], a.uin + 4 * P.off, a.fx + 4 * P.off, a.fy + 4 * P.off, it.z, it.w, sm);
+        xy_tile(bgeom(a, P), a.wtab[P.wc], a.uin + 4 * P.off, a.fx + 4 * P.off, a.fy + 4 * P.off, it.z, it.w, sm, false);
     }
 }
 
