@@ -417,7 +417,13 @@ int gpmood_batch_advance(gpmood_batch* b, int nsteps) {
         b->steps++;
         b->detected += b->hntrb[4];
         if (b->hntrb[6]) b->status |= GPM_STATUS_NAN;  // a NaN or inadmissible state left at order 1
-        if (b->hbar->err) return bfail(b, GPMOOD_E_CUDA, "batched MOOD loop: grid barrier timed out");
+        if (b->hbar->err) {  // clear the barrier and the aborted loop's pass stamps; the batch stays usable
+            cudaMemsetAsync(b->bar, 0, sizeof(GridBar), s);
+            cudaMemsetAsync(b->stamp, 0, (size_t)b->ncell * sizeof(unsigned), s);
+            cudaStreamSynchronize(s);
+            b->status |= GPM_STATUS_BARRIER;
+            return bfail(b, GPMOOD_E_CUDA, "batched MOOD loop: grid barrier timed out");
+        }
         if (b->hntrb[3]) {
             b->status |= GPM_STATUS_MOODCAP;
             return bfail(b, GPMOOD_E_MOOD_CAP, "batched MOOD loop hit max_mood_iters");

@@ -121,7 +121,8 @@ enum { GPM_STATUS_NAN = 1, GPM_STATUS_MOODCAP = 2, GPM_STATUS_DT = 4, GPM_STATUS
 // Grid barrier state of the cooperative MOOD-loop kernel (zeroed device memory).
 struct GridBar {
     unsigned count, gen;
-    int err, pad;
+    int err;
+    int limit;  // polls a waiting CTA makes before it gives up; 0: the default, ~1 s (test hook)
 };
 
 // Launch-time arguments of one RK stage.

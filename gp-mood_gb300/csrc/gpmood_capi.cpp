@@ -53,6 +53,7 @@ struct gpmood_ctx {
     int hvCap;
     float hvKeep;
     unsigned hvSeed;
+    int wait_limit;               // test hook: polls of the kernels' bounded waits (0: ~1 s)
     bool timing;                  // per-kernel CUDA-event timing
     bool trace;                   // GPMOOD_TRACE=1: one line per step on stderr
     cudaEvent_t ev[GPM_MAXST][4]; // per RK stage: flux, update, MOOD loop boundaries
@@ -337,11 +338,19 @@ int run_step(gpmood_ctx* c, double* u, double* ur, bool with_cfl) {
     c->ctr.steps++;
     c->ctr.status_flags |= c->hSc->status;
     if (c->hBar->err) {
+        c->ctr.status_flags |= GPM_STATUS_BARRIER;
+        // the aborted loop left its pass stamps without advancing the stamp
+        // epoch: clear both with the barrier, so that the next loop's pass ids
+        // cannot collide with them
         cudaMemsetAsync(c->dBar, 0, sizeof(GridBar), s);
+        if (c->wait_limit) cudaMemcpyAsync(&c->dBar->limit, &c->wait_limit, sizeof(int), cudaMemcpyHostToDevice, s);
+        cudaMemsetAsync(c->dStamp, 0, c->ncell * sizeof(unsigned), s);
+        cudaMemsetAsync(&c->dSc->stamp_epoch, 0, sizeof(unsigned), s);
         cudaStreamSynchronize(s);
         return fail(c, GPMOOD_E_CUDA, "MOOD loop: grid barrier timed out");
     }
     if (c->hSc->status & GPM_STATUS_TENSOR) return fail(c, GPMOOD_E_CUDA, "NN gate: tensor-core wait timed out");
+    if (c->hSc->status & GPM_STATUS_TMA) return fail(c, GPMOOD_E_CUDA, "first pass: TMA tile copy wait timed out");
     if (c->hSc->status & GPM_STATUS_MOODCAP) {
         const long long cap = c->p.max_mood_iters > 0 ? c->p.max_mood_iters : 2LL * c->p.lf * c->p.nf + 2;
         return fail(c, GPMOOD_E_MOOD_CAP, "MOOD loop did not converge in %lld passes", cap);
@@ -890,6 +899,16 @@ int gpmood_nn_gate_logits(gpmood_ctx* c, float* d_logits) {
     CU(cudaMemcpyAsync(&st, &c->dSc->status, sizeof st, cudaMemcpyDeviceToHost, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     if (st & GPM_STATUS_TENSOR) return fail(c, GPMOOD_E_CUDA, "NN gate: tensor-core wait timed out");
+    return 0;
+}
+
+int gpmood_set_wait_limit(gpmood_ctx* c, int polls) {
+    if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
+    if (polls < 0) return fail(c, GPMOOD_E_ARG, "polls must be >= 0 (0: the default bound)");
+    c->wait_limit = polls;
+    CU(cudaMemcpyAsync(&c->dBar->limit, &c->wait_limit, sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    if (c->nn) nn_gate_set_wait_limit(c->nn, polls);
     return 0;
 }
 

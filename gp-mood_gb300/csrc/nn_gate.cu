@@ -240,6 +240,24 @@ __device__ __forceinline__ bool tc_wait(unsigned long long* bar, uint32_t parity
     return false;
 }
 
+// The wait of the gate's MMAs: with limit > 0 (a test hook) at most `limit`
+// non-blocking polls; when that runs out, the MMAs still in flight are waited
+// for with the default bound before the caller frees the TMEM they write.
+__device__ __forceinline__ bool tc_wait_limited(unsigned long long* bar, uint32_t parity, int limit) {
+    if (limit <= 0) return tc_wait(bar, parity);
+    for (int it = 0; it < limit; it++) {
+        uint32_t done;
+        asm volatile(
+            "{\n.reg .pred p;\nmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\nselp.u32 %0, 1, 0, p;\n}\n"
+            : "=r"(done)
+            : "r"(smem_u32(bar)), "r"(parity)
+            : "memory");
+        if (done) return true;
+    }
+    tc_wait(bar, parity);
+    return false;
+}
+
 // 32 consecutive FP32 columns of this thread's TMEM lane.
 __device__ __forceinline__ void tc_ld32(uint32_t taddr, float* v) {
     uint32_t r[32];
@@ -265,7 +283,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_gate(GridGeom g, const double* _
                                                   const float* __restrict__ p, float thr, int8_t* __restrict__ order,
                                                   unsigned long long* __restrict__ count, int* __restrict__ list,
                                                   int* __restrict__ list_count, float* __restrict__ logits,
-                                                  int* __restrict__ status) {
+                                                  int* __restrict__ status, int wait_limit) {
     extern __shared__ __align__(1024) unsigned char smem_raw[];
     SmemTc& s = *reinterpret_cast<SmemTc*>(smem_raw);
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
@@ -338,7 +356,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_gate(GridGeom g, const double* _
             for (int k = 0; k < 3; k++) tc_mma(tmem, tc_desc(sx + 256 * k, 128, 768), tc_desc(sw0 + 256 * k, 128, 768), k > 0);
             tc_commit(&s.mbar);
         }
-        bool ok = tc_wait(&s.mbar, phase);
+        bool ok = tc_wait_limited(&s.mbar, phase, wait_limit);
         phase ^= 1;
         if (__syncthreads_or(!ok)) {
             timed_out = true;
@@ -371,7 +389,7 @@ __global__ void __launch_bounds__(TC_THREADS) k_gate(GridGeom g, const double* _
                 tc_mma(tmem + 64, tc_desc(sh + 256 * k, 128, 1024), tc_desc(sw1 + 256 * k, 128, 1024), k > 0);
             tc_commit(&s.mbar);
         }
-        ok = tc_wait(&s.mbar, phase);
+        ok = tc_wait_limited(&s.mbar, phase, wait_limit);
         phase ^= 1;
         if (__syncthreads_or(!ok)) {
             timed_out = true;
@@ -682,6 +700,7 @@ struct NnGate {
     float* params;
     float thr;
     bool loaded;
+    int wait_limit;  // polls of the MMA waits before a timeout (0: ~1 s); a test hook
 };
 
 NnGate* nn_gate_create(const GridGeom&) {
@@ -710,6 +729,7 @@ int nn_gate_set(NnGate* n, const float* params, cudaStream_t s) {
 }
 
 void nn_gate_set_threshold(NnGate* n, float thr) { n->thr = thr; }
+void nn_gate_set_wait_limit(NnGate* n, int polls) { n->wait_limit = polls; }
 
 bool nn_gate_loaded(const NnGate* n) { return n && n->loaded; }
 
@@ -730,7 +750,7 @@ int nn_gate_orders(NnGate* n, const GridGeom& g, const double* uin, int8_t* orde
     // persistent: 4 CTAs per SM, each holding 128 of the SM's 512 TMEM columns
     const int blocks = (int)(tiles < 4LL * nsm ? tiles : 4LL * nsm);
     k_gate<<<blocks, TC_THREADS, TC_SMEM, s>>>(g, uin, n->params, n->thr, order, count, list, list_count, logits,
-                                               status);
+                                               status, n->wait_limit);
     return cudaGetLastError() == cudaSuccess ? 1 : -1;
 }
 

@@ -33,6 +33,8 @@ void nn_gate_destroy(NnGate* n);
 // Upload FP32 parameters and pack the BF16 weight copies used by the kernels.
 int nn_gate_set(NnGate* n, const float* params, cudaStream_t s);
 void nn_gate_set_threshold(NnGate* n, float logit_threshold);
+// Test hook: the gate's MMA waits give up after `polls` polls (0: ~1 s).
+void nn_gate_set_wait_limit(NnGate* n, int polls);
 bool nn_gate_loaded(const NnGate* n);
 // Overwrite order[] of gated interior cells with mord-2; adds the number of
 // gated cells to *count and appends their padded indices to list (running

@@ -306,7 +306,7 @@ extern "C" int gpmood_time_stepping_noalloc(const gpmood_params* p, double* d_ui
     NCU(cudaMemcpyAsync(&hb, s.bar, sizeof hb, cudaMemcpyDeviceToHost, st));
     NCU(cudaStreamSynchronize(st));
     if (rc) return rc;
-    if (status) *status = h.status;
+    if (status) *status = h.status | (hb.err ? GPM_STATUS_BARRIER : 0);
     if (hb.err) return nerr(GPMOOD_E_CUDA, "MOOD loop grid barrier timed out");
     if (h.status & GPM_STATUS_MOODCAP) return nerr(GPMOOD_E_MOOD_CAP, "MOOD loop did not converge");
     return 0;

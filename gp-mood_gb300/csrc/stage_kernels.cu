@@ -945,6 +945,8 @@ __device__ __forceinline__ bool grid_sync(GridBar* b) {
     if (threadIdx.x == 0) {
         volatile unsigned* vgen = &b->gen;
         const unsigned g = *vgen;
+        const int lim = *(volatile int*)&b->limit;
+        const long long max_it = lim > 0 ? lim : (1LL << 24);  // ~1 s: far beyond any pass
         __threadfence();
         if (atomicAdd(&b->count, 1u) == gridDim.x - 1) {
             atomicExch(&b->count, 0u);
@@ -953,7 +955,7 @@ __device__ __forceinline__ bool grid_sync(GridBar* b) {
         } else {
             long long it = 0;
             while (*vgen == g) {
-                if (++it > (1LL << 24)) {  // ~1 s: far beyond any pass
+                if (++it > max_it) {
                     atomicExch(&b->err, 1);
                     break;
                 }

@@ -84,6 +84,7 @@ SIGNATURES = {
     "gpmood_time_stepping_dev": ([C.c_void_p, C.c_void_p, C.c_void_p, C.c_double, C.c_double], C.c_int),
     "gpmood_set_nn": ([C.c_void_p, C.POINTER(C.c_float), C.c_int], C.c_int),
     "gpmood_set_nn_threshold": ([C.c_void_p, C.c_float], C.c_int),
+    "gpmood_set_wait_limit": ([C.c_void_p, C.c_int], C.c_int),
     "gpmood_nn_ref_logits": ([C.c_void_p, C.c_void_p], C.c_int),
     "gpmood_nn_gate_logits": ([C.c_void_p, C.c_void_p], C.c_int),
     "gpmood_nn_predict": ([C.c_void_p, C.POINTER(C.c_byte), C.POINTER(C.c_longlong)], C.c_int),
@@ -337,6 +338,10 @@ class Solver:
     def nn_gate_logits(self, d_logits: int) -> None:
         """The gate's logit of every interior cell (device float array of lf*nf)."""
         self._check(self.lib.gpmood_nn_gate_logits(self._h, C.c_void_p(d_logits)))
+
+    def set_wait_limit(self, polls: int) -> None:
+        """Test hook: bound the kernels' spin-waits to `polls` polls (0: ~1 s)."""
+        self._check(self.lib.gpmood_set_wait_limit(self._h, int(polls)))
 
     def set_nn_threshold(self, logit_threshold: float) -> None:
         self._check(self.lib.gpmood_set_nn_threshold(self._h, float(logit_threshold)))

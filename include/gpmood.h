@@ -117,7 +117,8 @@ typedef struct gpmood_counters {
                                        state left in an order-1 cell (reported, the step
                                        still succeeds, as in the reference); bit 1: MOOD cap
                                        hit; bit 2: bad dt; bit 3: grid-barrier timeout;
-                                       bit 4: tensor-core wait timeout */
+                                       bit 4: tensor-core wait timeout; bit 5: TMA tile
+                                       copy wait timeout */
     long long kernel_launches;      /* kernels launched through this context */
 } gpmood_counters;
 
@@ -190,6 +191,16 @@ int  gpmood_get_orders(gpmood_ctx* ctx, signed char* orders);
  * stopping at tmax; *steps_done receives the steps taken (may be NULL). */
 int  gpmood_advance(gpmood_ctx* ctx, int nsteps, int* steps_done);
 int  gpmood_get_counters(const gpmood_ctx* ctx, gpmood_counters* out);
+
+/* Test hook for the failure paths; no counterpart in the reference.  Every
+ * spin-wait of the context's kernels is bounded (the grid barrier of the
+ * cooperative MOOD loop, the gate's tensor-core MMA waits): after ~1 s a wait
+ * gives up, sets a status bit (3 or 4 of gpmood_counters.status_flags) and the
+ * step fails with GPMOOD_E_CUDA, leaving the context usable.  This call bounds
+ * those waits to `polls` polls instead, so that a test can make them run out
+ * without a faulty GPU; 0 restores the default.  The gate frees its tensor
+ * memory only after the MMAs in flight have landed. */
+int  gpmood_set_wait_limit(gpmood_ctx* ctx, int polls);
 
 /* One step on device arrays (padded layout) on the context's stream; d_uin is
  * inout (its ghosts are refilled, as in the reference).  For callers that keep
