@@ -55,9 +55,11 @@ def parse():
     ap.add_argument("--batch-problems", type=int, default=1024)
     ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batched form (0: skip)")
     ap.add_argument("--adjoint", type=int, default=1, help="also time the adjoint form (0: skip)")
+    ap.add_argument("--dmr", type=int, default=1,
+                    help="also time whole DMR runs, plain against NN-gated, with their L1 errors (0: skip)")
     ap.add_argument("--final", action="store_true",
                     help="run plain (and NN-gated unless --nn 0) GP-MOOD from t=0 to t_final and compare them")
-    ap.add_argument("--case", choices=("sedov", "rp2d3", "dmr", "dmr_1024x256"), default="sedov",
+    ap.add_argument("--case", choices=tuple(FINAL_CASES), default="sedov",
                     help="problem of --final: Sedov n^2 (t_final 0.05), 2DRP3 256^2 (0.8), DMR 4096x1024 (0.2)")
     return ap.parse_args()
 
@@ -319,56 +321,68 @@ FINAL_CASES = {
     "rp2d3": ("rp2d3", 256, 256, 1.0, 1.0, 17, 0.8),
     "dmr": ("dmr", 4096, 1024, 4.0, 1.0, 35, 0.2),
     "dmr_1024x256": ("dmr", 1024, 256, 4.0, 1.0, 35, 0.2),
+    "dmr_256x64": ("dmr", 256, 64, 4.0, 1.0, 35, 0.2),
 }
+
+
+def whole_run(pkg, icname, lf, nf, lx, ly, bc, tfinal, fp, method, params=None, thr=0.0):
+    """One run from t = 0 to t_final, timed with CUDA events on the context's
+    stream; returns (figures, final state)."""
+    import torch
+    from gpmood_gb300 import ic
+    U0 = getattr(ic, icname)(lf, nf) if icname != "dmr" else ic.dmr(lf, nf, lx, ly)
+    with pkg.Solver(lf=lf, nf=nf, lx=lx, ly=ly, bc_type=bc, tmax=tfinal, fp_mode=fp, method=method) as s:
+        s.Boundary_C(U0, 0.0)
+        if method == pkg.NN_GP_MOOD:
+            s.set_nn(params)
+            s.set_nn_threshold(thr)
+        s.set_state(U0, 0.0)
+        s.set_timing(True)
+        stream = torch.cuda.ExternalStream(s.stream)
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        steps = s.advance(1 << 30)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        ms = ev0.elapsed_time(ev1)
+        U, t, _ = s.get_state()
+        c = s.counters()
+        tm = s.timing()
+    return ({"steps": steps, "t": t, "seconds": ms / 1e3, "value": lf * nf * steps / (ms * 1e-3),
+             "unit": "cell-updates/s", "detected_total": c.detected_total,
+             "max_passes_stage": c.max_passes_stage, "status_flags": c.status_flags,
+             "flux_share": tm.flux_ms / ms if ms else None, "mood_share": tm.mood_ms / ms if ms else None,
+             "mood_passes": tm.mood_passes,
+             "us_per_mood_pass": tm.mood_ms * 1e3 / tm.mood_passes if tm.mood_passes else None,
+             "final_state": {"sum_rho": float(U[4:-4, 4:-4, 0].sum()), "sum_E": float(U[4:-4, 4:-4, 3].sum())}},
+            U)
+
+
+def load_gate():
+    from gpmood_gb300 import nn_train as T
+    params = T.load_text(str(GATE))
+    meta_f = GATE.with_suffix(".json")
+    thr = float(json.loads(meta_f.read_text()).get("threshold", 0.0)) if meta_f.exists() else 0.0
+    return params, thr
 
 
 def run_final(args):
     """Plain (and, unless --nn 0, NN-gated) GP-MOOD from t = 0 to t_final on one
     of the benchmark problems: time to solution, steps, and the relative L1
     difference of the final states."""
-    import numpy as np
-    import torch
     import __graft_entry__ as ge
     pkg = ge.import_package()
-    from gpmood_gb300 import ic, nn_train as T
     icname, lf, nf, lx, ly, bc, tfinal = FINAL_CASES[args.case]
     lf = lf or args.n
     nf = nf or args.n
     fp = pkg.FP_FAST if args.fp_mode == "fast" else pkg.FP_EXACT
-    U0 = getattr(ic, icname)(lf, nf) if icname != "dmr" else ic.dmr(lf, nf, lx, ly)
-    params = T.load_text(str(GATE))
-    meta_f = GATE.with_suffix(".json")
-    thr = float(json.loads(meta_f.read_text()).get("threshold", 0.0)) if meta_f.exists() else 0.0
+    params, thr = load_gate()
     out = {}
     finals = {}
     variants = [("plain", pkg.GP_MOOD)] + ([("nn_gated", pkg.NN_GP_MOOD)] if args.nn else [])
     for name, method in variants:
-        with pkg.Solver(lf=lf, nf=nf, lx=lx, ly=ly, bc_type=bc, tmax=tfinal, fp_mode=fp, method=method) as s:
-            s.Boundary_C(U0, 0.0)
-            if method == pkg.NN_GP_MOOD:
-                s.set_nn(params)
-                s.set_nn_threshold(thr)
-            s.set_state(U0, 0.0)
-            s.set_timing(True)
-            stream = torch.cuda.ExternalStream(s.stream)
-            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            torch.cuda.synchronize()
-            ev0.record(stream)
-            steps = s.advance(1 << 30)
-            ev1.record(stream)
-            torch.cuda.synchronize()
-            ms = ev0.elapsed_time(ev1)
-            U, t, _ = s.get_state()
-            c = s.counters()
-            tm = s.timing()
-        finals[name] = U
-        out[name] = {"steps": steps, "t": t, "seconds": ms / 1e3, "value": lf * nf * steps / (ms * 1e-3),
-                     "unit": "cell-updates/s", "detected_total": c.detected_total,
-                     "max_passes_stage": c.max_passes_stage, "status_flags": c.status_flags,
-                     "flux_share": tm.flux_ms / ms if ms else None, "mood_share": tm.mood_ms / ms if ms else None,
-                     "mood_passes": tm.mood_passes,
-                     "us_per_mood_pass": tm.mood_ms * 1e3 / tm.mood_passes if tm.mood_passes else None,
-                     "final_state": {"sum_rho": float(U[4:-4, 4:-4, 0].sum()), "sum_E": float(U[4:-4, 4:-4, 3].sum())}}
+        out[name], finals[name] = whole_run(pkg, icname, lf, nf, lx, ly, bc, tfinal, fp, method, params, thr)
         # each variant on stderr as soon as it ends, so that a long run that is cut off still reports
         print(json.dumps({"partial": name, "case": args.case, **out[name]}), file=sys.stderr, flush=True)
     if args.nn:
@@ -380,6 +394,48 @@ def run_final(args):
             "fp_mode": args.fp_mode, "gate": GATE.name, "logit_threshold": thr, **out}
     print(json.dumps(line), flush=True)
     return 0
+
+
+def l1_density_error(U, Uref, lx, ly):
+    """sum |rho - R(rho_ref)| dx dy over the interior, R = the average of each
+    2x2 block of the twice finer reference run (the L1 error against a
+    converged solution, as the deprecated code's error() measures it)."""
+    import numpy as np
+    r = U[4:-4, 4:-4, 0]
+    f = Uref[4:-4, 4:-4, 0]
+    nf, lf = r.shape
+    R = f.reshape(nf, 2, lf, 2).mean(axis=(1, 3))
+    return float(np.abs(r - R).sum() * (lx / lf) * (ly / nf))
+
+
+def measure_dmr_whole_runs(pkg, fp):
+    """The oblique-shock (double Mach reflection) problem from t = 0 to 0.2, where
+    plain MOOD's cascade crawls for hundreds of passes per stage: plain and
+    NN-gated at 1024x256 (speed, final-state difference), and at 512x128 both
+    runs' L1 density error against the plain 1024x256 run (the error at which
+    the two speeds are compared)."""
+    if not GATE.exists():
+        return {"unavailable": f"no trained gate parameters ({GATE.name})"}
+    params, thr = load_gate()
+    lx, ly, bc, tf = 4.0, 1.0, 35, 0.2
+    out = {"workload": "double Mach reflection (Mach-10 oblique shock) on [0,4]x[0,1], t_final=0.2, plain GP-MOOD "
+                       "Mord=5 (R2->R1->1), ngp=3, ell=12dx, HLLC, SSP-RK3, CFL 0.8; the same with the BF16 gate",
+           "gate": GATE.name, "logit_threshold": thr}
+    fine = {}
+    for name, method in (("plain", pkg.GP_MOOD), ("nn_gated", pkg.NN_GP_MOOD)):
+        out[f"{name}_1024x256"], fine[name] = whole_run(pkg, "dmr", 1024, 256, lx, ly, bc, tf, fp, method, params, thr)
+    out["speedup_1024x256"] = out["plain_1024x256"]["seconds"] / out["nn_gated_1024x256"]["seconds"]
+    out["rel_l1_gated_vs_plain_1024x256"] = _rel_l1(fine["nn_gated"], fine["plain"])
+    errs = {}
+    for name, method in (("plain", pkg.GP_MOOD), ("nn_gated", pkg.NN_GP_MOOD)):
+        fig, U = whole_run(pkg, "dmr", 512, 128, lx, ly, bc, tf, fp, method, params, thr)
+        errs[name] = l1_density_error(U, fine["plain"], lx, ly)
+        out[f"{name}_512x128"] = {"seconds": fig["seconds"], "steps": fig["steps"], "value": fig["value"],
+                                  "l1_rho_vs_plain_1024x256": errs[name]}
+    out["speedup_512x128"] = out["plain_512x128"]["seconds"] / out["nn_gated_512x128"]["seconds"]
+    out["l1_ratio_gated_over_plain_512x128"] = errs["nn_gated"] / errs["plain"]
+    out["timing"] = "CUDA events on the context's stream around gpmood_advance to t_final"
+    return out
 
 
 def run_final_reference(args):
@@ -557,6 +613,8 @@ def run_ours(args, ws, rank, local):
         forms["batched"] = measure_batched(pkg, args.batch_problems, args.batch_steps, fp)
     if args.adjoint:
         forms["adjoint"] = measure_adjoint(pkg)
+    if args.dmr and args.nn:
+        forms["dmr_whole_runs"] = measure_dmr_whole_runs(pkg, fp)
 
     cpu = None
     if rank == 0 and ws == 1 and args.cpu_steps > 0:

@@ -88,6 +88,7 @@ struct GridGeom {
     int num_flux;        // 100 HLLC, 101 LLF, 102 HLL, 103 unsplit
     int mood_solo;       // device MOOD loop: lists of at most this many cells run in one CTA
     int flux_tma;        // fast first pass: halo tiles staged by a TMA bulk tensor copy (1) or loads (0)
+    int solo_split;      // one-CTA MOOD passes: DETECTION split over warp roles (1) or per cell (0)
     int cc_col;          // NN_GP_MOOD_CC: the column l whose order-3 states are blended (-1: none)
 };
 
@@ -99,6 +100,10 @@ int gpm_mood_solo_default();
 // selects the plain-load staging (A/B timing only: the staged tile, and so
 // every result, is the same either way).  Read at context creation.
 int gpm_flux_tma_default();
+
+// Default of GridGeom::solo_split (1); GPMOOD_SOLO_SPLIT=0 keeps DETECTION on
+// one thread per cross cell (A/B timing only: the decisions are the same).
+int gpm_solo_split_default();
 
 // Scalars that stay on the device across a step.
 struct DevScalars {

@@ -79,6 +79,11 @@ int gpm_flux_tma_default() {
     return e && *e ? (atoi(e) != 0) : 1;
 }
 
+int gpm_solo_split_default() {
+    const char* e = getenv("GPMOOD_SOLO_SPLIT");
+    return e && *e ? (atoi(e) != 0) : 1;
+}
+
 namespace {
 
 // NVTX range over a host scope (steps and stages show up on an Nsight Systems
@@ -489,6 +494,7 @@ int gpmood_create(const gpmood_params* p, gpmood_ctx** out) {
     c->g.num_flux = p->num_flux;
     c->g.mood_solo = gpm_mood_solo_default();
     c->g.flux_tma = gpm_flux_tma_default();
+    c->g.solo_split = gpm_solo_split_default();
     c->g.cc_col = -1;
     c->nstages = p->integrator == GPMOOD_FE ? 1 : p->integrator == GPMOOD_SSP_RK2 ? 2 : p->integrator == GPMOOD_SSP_RK4 ? 5 : 3;
     c->g.dmp = p->dmp;

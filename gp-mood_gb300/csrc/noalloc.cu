@@ -271,6 +271,7 @@ extern "C" int gpmood_time_stepping_noalloc(const gpmood_params* p, double* d_ui
     g.u2_tol = p->u2_tol;
     g.mood_solo = gpm_mood_solo_default();
     g.flux_tma = gpm_flux_tma_default();
+    g.solo_split = gpm_solo_split_default();
     g.cc_col = -1;
     GpWeights w;
     if (weights_for(p, &w)) return nerr(GPMOOD_E_ARG, "GP precompute rejected the knobs");

@@ -448,43 +448,62 @@ __device__ __forceinline__ bool inadmissible(const Cell& uo) {
 #endif
 }
 
-// DETECTION checks for one interior cell (mod_subroutine_MOOD.f90:41-131).
-// uin points at Uin(1, l, n) of a padded array of row pitch 4*nx doubles.
-// The DMP bounds test runs before the shock detector: both are side-effect
-// free and combined by .and., so the decision is the reference's.
-__device__ __forceinline__ bool mood_troubled(const Cell& uo, const double* __restrict__ uin, int nx,
-                                              const GridGeom& g, const double* d2x, const double* d2y) {
-    if (le_zero_or_nan(uo.r)) return true;
+// DETECTION checks for one interior cell (mod_subroutine_MOOD.f90:41-131),
+// in three parts that the MOOD loop may evaluate on different warps:
+//   mood_uout_part  the tests that read Uout: positivity (:43-51) and the DMP
+//                   bounds with the plateau test (:55-70); 0 passes, 1
+//                   troubled, 2 the DMP bound is violated;
+//   mood_shock_part the shock detector (:53, :191-238), on Uin only;
+//   mood_u2_smooth  the U2 smooth-extremum test in x or in y (:74-119), on
+//                   Uin only: GP second derivatives of rho at the 5 cross
+//                   cells, each from that cell's own 5-point cross.
+// A cell is troubled iff part 1 says 1, or it says 2, the shock detector
+// fires and, with U2 on, neither direction is smooth.  Every part is side
+// effect free, so evaluating them in any order, or all of them, gives the
+// reference's decision.  uin points at Uin(1, l, n) of a padded array of row
+// pitch 4*nx doubles.
+__device__ __forceinline__ int mood_uout_part(const Cell& uo, const double* __restrict__ uin, int nx,
+                                              const GridGeom& g) {
+    if (le_zero_or_nan(uo.r)) return 1;
 #if GPM_EXACT
     const double p = pressure(uo);
 #else
     const double p = pressure_ir(uo, gpm_fast_rcp(uo.r));
 #endif
-    if (le_zero_or_nan(p)) return true;
-    if (!g.dmp) return false;
+    if (le_zero_or_nan(p)) return 1;
+    if (!g.dmp) return 0;
+    const size_t row = (size_t)4 * nx;
+    const double c = __ldg(uin), l = __ldg(uin - 4), r = __ldg(uin + 4), b = __ldg(uin - row), t = __ldg(uin + row);
+    const double mn = fmin(fmin(fmin(fmin(c, l), b), t), r);
+    const double mx = fmax(fmax(fmax(fmax(c, l), b), t), r);
+    const double Mm = mx - mn;
+    if (!(Mm > g.dx * g.dx * g.dx)) return 0;          // plateau, :68
+    return ((uo.r > mx) || (uo.r < mn)) ? 2 : 0;        // :70
+}
+
+__device__ __forceinline__ bool mood_shock_part(const double* __restrict__ uin, int nx, const GridGeom& g) {
     const size_t row = (size_t)4 * nx;
     const Cell C = ld_cell(uin), Lc = ld_cell(uin - 4), Rc = ld_cell(uin + 4);
     const Cell Bc = ld_cell(uin - row), Tc = ld_cell(uin + row);
-    const double mn = fmin(fmin(fmin(fmin(C.r, Lc.r), Bc.r), Tc.r), Rc.r);
-    const double mx = fmax(fmax(fmax(fmax(C.r, Lc.r), Bc.r), Tc.r), Rc.r);
-    const double Mm = mx - mn;
-    if (!(Mm > g.dx * g.dx * g.dx)) return false;                 // plateau, :68
-    if (!((uo.r > mx) || (uo.r < mn))) return false;              // :70
-    if (!shock_detector(C, Lc, Rc, Bc, Tc, g.dx, g.dy)) return false;
-    if (!g.u2) return true;
-    // U2 smooth-extremum test, :74-119: GP second derivatives of rho at the
-    // 5 cross cells, each from that cell's own 5-point cross.
-    double D2x[5], D2y[5];
+    return shock_detector(C, Lc, Rc, Bc, Tc, g.dx, g.dy);
+}
+
+// DIR 0: the x test on D2x, 1: the y test on D2y.
+template <int DIR>
+__device__ __forceinline__ bool mood_u2_smooth(const double* __restrict__ uin, int nx, const GridGeom& g,
+                                               const double* d2) {
+    const size_t row = (size_t)4 * nx;
     const int ci_[5] = {-1, 0, 1, 0, 0}, cj_[5] = {0, 0, 0, -1, 1};  // (-1,0),(0,0),(1,0),(0,-1),(0,1)
+    double D[5];
     if (g.u2_fd) {
         // POL_MOOD (:81-84): dot_product((1,-2,1), rho(l+i-1:l+i+1, n+j))/dx**2;
         // 1*a and -2*b are exact, so the sum is (a - 2b) + c in either FP mode.
+        const ptrdiff_t step = DIR == 0 ? 4 : (ptrdiff_t)row;
+        const double h = DIR == 0 ? g.dx : g.dy;
 #pragma unroll
         for (int s = 0; s < 5; s++) {
             const double* base = uin + (ptrdiff_t)4 * ci_[s] + (ptrdiff_t)row * cj_[s];
-            const double m = __ldg(base);
-            D2x[s] = ((__ldg(base - 4) + -2. * m) + __ldg(base + 4)) / (g.dx * g.dx);
-            D2y[s] = ((__ldg(base - row) + -2. * m) + __ldg(base + row)) / (g.dy * g.dy);
+            D[s] = ((__ldg(base - step) + -2. * __ldg(base)) + __ldg(base + step)) / (h * h);
         }
     } else {
 #pragma unroll
@@ -493,24 +512,24 @@ __device__ __forceinline__ bool mood_troubled(const Cell& uo, const double* __re
             double q[5];
 #pragma unroll
             for (int k = 0; k < 5; k++) q[k] = __ldg(base + (ptrdiff_t)4 * st_ox(k) + (ptrdiff_t)row * st_oy(k));
-            double sx = d2x[0] * q[0], sy = d2y[0] * q[0];
+            double sum = d2[0] * q[0];
 #pragma unroll
-            for (int k = 1; k < 5; k++) {
-                sx = sx + d2x[k] * q[k];
-                sy = sy + d2y[k] * q[k];
-            }
-            D2x[s] = sx;
-            D2y[s] = sy;
+            for (int k = 1; k < 5; k++) sum = sum + d2[k] * q[k];
+            D[s] = sum;
         }
     }
-    const double Xmin = fmin(fmin(fmin(fmin(D2x[0], D2x[1]), D2x[2]), D2x[3]), D2x[4]);
-    const double Xmax = fmax(fmax(fmax(fmax(D2x[0], D2x[1]), D2x[2]), D2x[3]), D2x[4]);
-    const double Ymin = fmin(fmin(fmin(fmin(D2y[0], D2y[1]), D2y[2]), D2y[3]), D2y[4]);
-    const double Ymax = fmax(fmax(fmax(fmax(D2y[0], D2y[1]), D2y[2]), D2y[3]), D2y[4]);
+    const double Xmin = fmin(fmin(fmin(fmin(D[0], D[1]), D[2]), D[3]), D[4]);
+    const double Xmax = fmax(fmax(fmax(fmax(D[0], D[1]), D[2]), D[3]), D[4]);
     const double delta = g.u2_tol ? fmax(g.dx, g.dy) : 0.0;
-    if ((Xmin * Xmax > -delta) && ((fmax(fabs(Xmin), fabs(Xmax)) < delta) || (fabs(Xmin / Xmax) >= 1. / 2)))
-        return false;
-    if ((Ymin * Ymax > -delta) && ((fmax(fabs(Ymin), fabs(Ymax)) < delta) || (fabs(Ymin / Ymax) >= 1. / 2)))
-        return false;
-    return true;
+    return (Xmin * Xmax > -delta) && ((fmax(fabs(Xmin), fabs(Xmax)) < delta) || (fabs(Xmin / Xmax) >= 1. / 2));
+}
+
+__device__ __forceinline__ bool mood_troubled(const Cell& uo, const double* __restrict__ uin, int nx,
+                                              const GridGeom& g, const double* d2x, const double* d2y) {
+    const int r = mood_uout_part(uo, uin, nx, g);
+    if (r != 2) return r == 1;
+    if (!mood_shock_part(uin, nx, g)) return false;
+    if (!g.u2) return true;
+    if (mood_u2_smooth<0>(uin, nx, g, d2x)) return false;
+    return !mood_u2_smooth<1>(uin, nx, g, d2y);
 }

@@ -983,9 +983,78 @@ __device__ __forceinline__ bool mood_sync(GridBar* b, bool solo) {
     return grid_sync(b);
 }
 
+// The cross phase of a pass run by one CTA (solo).  A lone warp pays ~64
+// cycles for every FP64 instruction, so one cross cell's DETECTION chain
+// (update, positivity, DMP bounds, shock detector, U2 in x and in y) is what
+// a short pass waits on.  Its parts are split over four warp roles that run
+// at once on every cross cell of a chunk: role 0 updates Uout and runs the
+// Uout tests (mood_uout_part), roles 1-3 the Uin-only shock detector and the
+// two U2 tests; after a CTA barrier role 0 combines them, lowers the order of
+// a troubled cell and lists it.  The decision is mood_troubled's.
+constexpr int SOLO_CHUNK = MOOD_THREADS / 4;  // cross cells per chunk (one per lane of each role)
+
+struct SoloCross {
+    int cell[SOLO_CHUNK];
+    int8_t part[SOLO_CHUNK];      // mood_uout_part; -1: ghost cell or already updated in this pass
+    bool flag[3][SOLO_CHUNK];     // shock, U2 smooth in x, U2 smooth in y
+};
+
+__device__ __forceinline__ void solo_cross(const StageArgs& a, const GpWeights& w, int cur, int nt, unsigned pid,
+                                           SoloCross& sm) {
+    const GridGeom& g = a.g;
+    const double qx = a.sc->qx, qy = a.sc->qy;
+    const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int role = warp & 3, j = (warp >> 2) * 32 + lane;  // item of the chunk
+    const int nxt = cur ^ 1, total = 5 * nt;
+    for (int base = 0; base < total; base += SOLO_CHUNK) {
+        const int i = base + j;
+        if (i < total) {
+            const size_t t = (size_t)a.tlist[cur][i / 5];
+            const int k = i % 5;
+            const size_t c = k == 0 ? t - g.nx : k == 1 ? t - 1 : k == 2 ? t : k == 3 ? t + 1 : t + g.nx;
+            const int l = (int)(c % (size_t)g.nx) - 3, n = (int)(c / (size_t)g.nx) - 3;
+            const bool interior = l >= 1 && l <= g.lf && n >= 1 && n <= g.nf;
+            const double* uin = a.uin + 4 * c;
+            if (role == 0) {
+                int r = -1;
+                if (interior && atomicExch(&a.stamp[c], pid) != pid) {
+                    const Cell uo = cell_update(g, a.uin, a.fx, a.fy, c, qx, qy);
+                    st_cell(a.uout + 4 * c, uo);
+                    if (a.order[c] > 1) {
+                        r = mood_uout_part(uo, uin, g.nx, g);
+                    } else {
+                        if (inadmissible(uo)) atomicOr(&a.sc->status, GPM_STATUS_NAN);
+                        r = 0;
+                    }
+                }
+                sm.cell[j] = (int)c;
+                sm.part[j] = (int8_t)r;
+            } else if (interior) {
+                sm.flag[role - 1][j] = role == 1   ? mood_shock_part(uin, g.nx, g)
+                                       : role == 2 ? mood_u2_smooth<0>(uin, g.nx, g, w.d2x)
+                                                   : mood_u2_smooth<1>(uin, g.nx, g, w.d2y);
+            }
+        }
+        __syncthreads();
+        if (role == 0) {
+            bool trb = false;
+            int cval = 0;
+            if (i < total && sm.part[j] >= 0) {
+                const int r = sm.part[j];
+                cval = sm.cell[j];
+                trb = r == 1 || (r == 2 && sm.flag[0][j] && !(g.u2 && (sm.flag[1][j] || sm.flag[2][j])));
+            }
+            if (trb) cascade_order(&a.order[cval]);
+            list_append(trb, a.tlist[nxt], &a.sc->ntrb[nxt], cval);
+        }
+        __syncthreads();
+    }
+}
+
 template <int NGP>
 __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, const __grid_constant__ GpWeights w, GridBar* bar,
                                                       int max_pass, int stage) {
+    __shared__ SoloCross solo_sm;
     const GridGeom& g = a.g;
     const double qx = a.sc->qx, qy = a.sc->qy;
     const unsigned epoch = a.sc->stamp_epoch;  // stamps epoch+2, epoch+3, ... are new
@@ -1022,6 +1091,11 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
         if (!mood_sync(bar, solo)) return;
         // the 5-point crosses: Uout from Uin and the current fluxes, DETECTION
         const unsigned pid = epoch + (unsigned)pass;
+        if (solo && g.solo_split) {
+            solo_cross(a, w, cur, nt, pid, solo_sm);
+            cur ^= 1;
+            continue;
+        }
         const int nxt = cur ^ 1, total = 5 * nt;
         const int lim = ((total + wstride - 1) / wstride) * wstride;
         for (int base = 0; base < lim; base += wstride) {
@@ -1277,6 +1351,7 @@ __device__ __forceinline__ GridGeom bgeom(const BatchArgs& a, const BProb& p) {
     g.dmp = a.dmp; g.u2 = a.u2; g.u2_tol = a.u2_tol; g.u2_fd = 0; g.num_flux = a.num_flux;
     g.mood_solo = a.mood_solo;
     g.flux_tma = 0;
+    g.solo_split = 0;
     g.cc_col = -1;
     return g;
 }

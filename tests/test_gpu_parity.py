@@ -283,3 +283,27 @@ def test_fast_first_pass_tma_and_load_staging_agree(pkg, oracle, case, monkeypat
     assert sa == sb == 0
     assert ta == tb and np.array_equal(ma, mb)
     assert nan_equal(Ua, Ub)
+
+
+@pytest.mark.parametrize("fp", ["exact", "fast"])
+def test_solo_mood_passes_split_detection_agrees(pkg, oracle, fp, monkeypatch):
+    """One-CTA MOOD passes split DETECTION over warp roles (default) or keep
+    it on one thread per cross cell (GPMOOD_SOLO_SPLIT=0): the decisions and
+    so the runs are the same, bit for bit, on the DMR crawl."""
+    ic, lf, nf, kn = CASES["dmr"]
+    p = _oracle_params(oracle, lf, nf, kn)
+    U0 = oracle.initial_condition(p, ic)
+    mode = pkg.FP_EXACT if fp == "exact" else pkg.FP_FAST
+    out = []
+    for split in ("1", "0"):
+        monkeypatch.setenv("GPMOOD_SOLO_SPLIT", split)
+        with _solver(pkg, lf, nf, mode, kn) as s:
+            s.set_state(U0, 0.0)
+            assert s.advance(8) == 8
+            U, t, _ = s.get_state()
+            c = s.counters()
+            out.append((U, t, s.orders(), c.detected_total, c.max_passes_stage))
+    (Ua, ta, ma, da, pa), (Ub, tb, mb, db, pb) = out
+    assert (ta, da, pa) == (tb, db, pb) and pa > 2
+    assert np.array_equal(ma, mb)
+    assert nan_equal(Ua, Ub)
