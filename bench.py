@@ -55,6 +55,10 @@ def parse():
     ap.add_argument("--batch-problems", type=int, default=1024)
     ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batched form (0: skip)")
     ap.add_argument("--adjoint", type=int, default=1, help="also time the adjoint form (0: skip)")
+    ap.add_argument("--repair", type=int, default=0,
+                    help="with --final: also the NN-gated run with the gate's extras repair (gpmood_set_nn_repair)")
+    ap.add_argument("--l1-ref", type=int, default=0,
+                    help="with --final: also the plain run on the twice finer grid, and both runs' L1 errors against it")
     ap.add_argument("--dmr", type=int, default=1,
                     help="also time whole DMR runs, plain against NN-gated, with their L1 errors (0: skip)")
     ap.add_argument("--final", action="store_true",
@@ -325,7 +329,7 @@ FINAL_CASES = {
 }
 
 
-def whole_run(pkg, icname, lf, nf, lx, ly, bc, tfinal, fp, method, params=None, thr=0.0):
+def whole_run(pkg, icname, lf, nf, lx, ly, bc, tfinal, fp, method, params=None, thr=0.0, repair=False):
     """One run from t = 0 to t_final, timed with CUDA events on the context's
     stream; returns (figures, final state)."""
     import torch
@@ -336,6 +340,7 @@ def whole_run(pkg, icname, lf, nf, lx, ly, bc, tfinal, fp, method, params=None, 
         if method == pkg.NN_GP_MOOD:
             s.set_nn(params)
             s.set_nn_threshold(thr)
+            s.set_nn_repair(repair)
         s.set_state(U0, 0.0)
         s.set_timing(True)
         stream = torch.cuda.ExternalStream(s.stream)
@@ -380,14 +385,25 @@ def run_final(args):
     params, thr = load_gate()
     out = {}
     finals = {}
-    variants = [("plain", pkg.GP_MOOD)] + ([("nn_gated", pkg.NN_GP_MOOD)] if args.nn else [])
-    for name, method in variants:
-        out[name], finals[name] = whole_run(pkg, icname, lf, nf, lx, ly, bc, tfinal, fp, method, params, thr)
+    variants = [("plain", pkg.GP_MOOD, False)] + ([("nn_gated", pkg.NN_GP_MOOD, False)] if args.nn else [])
+    if args.nn and args.repair:
+        variants.append(("nn_gated_repaired", pkg.NN_GP_MOOD, True))
+    for name, method, repair in variants:
+        out[name], finals[name] = whole_run(pkg, icname, lf, nf, lx, ly, bc, tfinal, fp, method, params, thr, repair)
         # each variant on stderr as soon as it ends, so that a long run that is cut off still reports
         print(json.dumps({"partial": name, "case": args.case, **out[name]}), file=sys.stderr, flush=True)
     if args.nn:
         out["nn_gated"]["speedup_vs_plain"] = out["plain"]["seconds"] / out["nn_gated"]["seconds"]
         out["rel_l1_final"] = _rel_l1(finals["nn_gated"], finals["plain"])
+    if "nn_gated_repaired" in out:
+        out["nn_gated_repaired"]["speedup_vs_plain"] = out["plain"]["seconds"] / out["nn_gated_repaired"]["seconds"]
+        out["nn_gated_repaired"]["rel_l1_vs_plain"] = _rel_l1(finals["nn_gated_repaired"], finals["plain"])
+    if args.l1_ref:
+        # L1 density errors against the plain run on the twice finer grid
+        ref, Uref = whole_run(pkg, icname, 2 * lf, 2 * nf, lx, ly, bc, tfinal, fp, pkg.GP_MOOD, params, thr)
+        out["l1_reference"] = {"grid": f"{2 * lf}x{2 * nf}", "seconds": ref["seconds"], "steps": ref["steps"]}
+        for name in finals:
+            out[name]["l1_rho_vs_2x_plain"] = l1_density_error(finals[name], Uref, lx, ly)
     line = {"metric": "time to t_final", "case": args.case,
             "workload": f"{icname} {lf}x{nf} on [0,{lx:g}]x[0,{ly:g}], BC {bc}, t_final={tfinal}, plain GP-MOOD "
                         f"Mord=5 (R2->R1->1), ngp=3, ell=12dx, HLLC, SSP-RK3, CFL 0.8",

@@ -169,6 +169,8 @@ struct KernelTable {
     // y = sum c[i]*x[i], i < n <= 5, left to right; optionally the Setdt reduction of y
     void (*lincomb)(const GridGeom& g, double* y, int n, const double* const* x, const double* c, int with_cfl,
                     DevScalars* sc, cudaStream_t s);
+    // the gate's extras repair on the gated list tlist[1] (at most max_items cells)
+    void (*gate_repair)(const StageArgs& a, const GpWeights& w, int max_items, cudaStream_t s);
 };
 
 namespace gpm_exact { extern const KernelTable table; }

@@ -54,6 +54,7 @@ struct gpmood_ctx {
     float hvKeep;
     unsigned hvSeed;
     int wait_limit;               // test hook: polls of the kernels' bounded waits (0: ~1 s)
+    bool nn_repair;               // the gate's extras repair (gpmood_set_nn_repair)
     bool timing;                  // per-kernel CUDA-event timing
     bool trace;                   // GPMOOD_TRACE=1: one line per step on stderr
     cudaEvent_t ev[GPM_MAXST][4]; // per RK stage: flux, update, MOOD loop boundaries
@@ -189,6 +190,10 @@ int run_stage(gpmood_ctx* c, double* uin, double* uout, int stage, int bc_stage)
     au.uniform_order = nnref ? 0 : 1;
     c->flux_nl[stage] = kt.flux_all(au, c->w, s);
     if (fixup) {
+        if (c->nn_repair) {
+            kt.gate_repair(a, c->w, c->p.lf * c->p.nf, s);
+            c->ctr.kernel_launches += 1;
+        }
         kt.mood_faces(a, c->w, 1, c->p.lf * c->p.nf, s);
         c->ctr.kernel_launches += 1;
     }
@@ -915,6 +920,12 @@ int gpmood_set_wait_limit(gpmood_ctx* c, int polls) {
     CU(cudaMemcpyAsync(&c->dBar->limit, &c->wait_limit, sizeof(int), cudaMemcpyHostToDevice, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     if (c->nn) nn_gate_set_wait_limit(c->nn, polls);
+    return 0;
+}
+
+int gpmood_set_nn_repair(gpmood_ctx* c, int on) {
+    if (!c) return fail(nullptr, GPMOOD_E_ARG, "ctx is NULL");
+    c->nn_repair = on != 0;
     return 0;
 }
 

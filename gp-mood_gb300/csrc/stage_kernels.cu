@@ -1188,6 +1188,29 @@ void launch_mood_cells(const StageArgs& a, const GpWeights& w, int cur, int max_
     k_mood_cells<<<list_grid(5 * max_trb, 256), 256, 0, s>>>(a, w, cur, pass_id);
 }
 
+// The gate's extras repair (optional): a gated cell whose update from the
+// uniform first pass (every face at mord, already stored) passes DETECTION is
+// given mord back before the gated cells' faces are recomputed, so that only
+// cells plain MOOD would also flag in its first pass start lowered.  The
+// a-priori count drops by the cells given back.
+__global__ void __launch_bounds__(256) k_gate_repair(StageArgs a, const __grid_constant__ GpWeights w) {
+    const GridGeom& g = a.g;
+    const int n = a.sc->ntrb[1];
+    const double qx = a.sc->qx, qy = a.sc->qy;
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+        const size_t c = (size_t)a.tlist[1][i];
+        const Cell uo = cell_update(g, a.uin, a.fx, a.fy, c, qx, qy);
+        if (!mood_troubled(uo, a.uin + 4 * c, g.nx, g, w.d2x, w.d2y)) {
+            a.order[c] = (int8_t)g.mord;
+            atomicAdd(&a.sc->apriori_step, ~0ull);  // minus one
+        }
+    }
+}
+
+void launch_gate_repair(const StageArgs& a, const GpWeights& w, int max_items, cudaStream_t s) {
+    k_gate_repair<<<list_grid(max_items, 256), 256, 0, s>>>(a, w);
+}
+
 // ---------------------------------------------------------------------------
 // Setdt (physics.f90:78-129): min over every cell, ghosts included, of
 // 1/(1/(dx/(|u|+c)) + 1/(dy/(|v|+c))).  Reduced with fmin inside a CTA and an
@@ -1330,7 +1353,8 @@ void launch_advance_t(DevScalars* sc, cudaStream_t s) { k_advance_t<<<1, 1, 0, s
 
 const KernelTable table = {launch_bc,          launch_flux_all,   launch_update_detect, launch_mood_mark,
                            launch_mood_faces,  launch_mood_cells, launch_combine,       launch_cfl,
-                           launch_dt_finalize, launch_advance_t,  launch_mood_loop,     launch_lincomb};
+                           launch_dt_finalize, launch_advance_t,  launch_mood_loop,     launch_lincomb,
+                           launch_gate_repair};
 
 }  // namespace GPM_NS
 

@@ -85,6 +85,7 @@ SIGNATURES = {
     "gpmood_set_nn": ([C.c_void_p, C.POINTER(C.c_float), C.c_int], C.c_int),
     "gpmood_set_nn_threshold": ([C.c_void_p, C.c_float], C.c_int),
     "gpmood_set_wait_limit": ([C.c_void_p, C.c_int], C.c_int),
+    "gpmood_set_nn_repair": ([C.c_void_p, C.c_int], C.c_int),
     "gpmood_nn_ref_logits": ([C.c_void_p, C.c_void_p], C.c_int),
     "gpmood_nn_gate_logits": ([C.c_void_p, C.c_void_p], C.c_int),
     "gpmood_nn_predict": ([C.c_void_p, C.POINTER(C.c_byte), C.POINTER(C.c_longlong)], C.c_int),
@@ -338,6 +339,10 @@ class Solver:
     def nn_gate_logits(self, d_logits: int) -> None:
         """The gate's logit of every interior cell (device float array of lf*nf)."""
         self._check(self.lib.gpmood_nn_gate_logits(self._h, C.c_void_p(d_logits)))
+
+    def set_nn_repair(self, on: bool) -> None:
+        """The gate's extras repair: gated cells that pass DETECTION at Mord get Mord back."""
+        self._check(self.lib.gpmood_set_nn_repair(self._h, int(bool(on))))
 
     def set_wait_limit(self, polls: int) -> None:
         """Test hook: bound the kernels' spin-waits to `polls` polls (0: ~1 s)."""

@@ -192,6 +192,14 @@ int  gpmood_get_orders(gpmood_ctx* ctx, signed char* orders);
 int  gpmood_advance(gpmood_ctx* ctx, int nsteps, int* steps_done);
 int  gpmood_get_counters(const gpmood_ctx* ctx, gpmood_counters* out);
 
+/* The gate's extras repair (BF16 gate, method NN_GP_MOOD with nn_reference 0);
+ * no counterpart in the reference.  With on != 0, a cell the gate starts at
+ * Mord-2 whose update from the uniform first pass passes DETECTION gets Mord
+ * back before the stage continues: only cells that plain MOOD's first
+ * DETECTION also flags start lowered, trading the gate's saved passes for a
+ * solution closer to plain GP-MOOD.  Off by default. */
+int  gpmood_set_nn_repair(gpmood_ctx* ctx, int on);
+
 /* Test hook for the failure paths; no counterpart in the reference.  Every
  * spin-wait of the context's kernels is bounded (the grid barrier of the
  * cooperative MOOD loop, the gate's tensor-core MMA waits): after ~1 s a wait

@@ -197,3 +197,41 @@ def test_training_on_plain_mood_labels_and_gate_gain(pkg):
     I = (slice(4, -4), slice(4, -4), 0)
     rel = np.abs(Ug[I] - Up[I]).sum() / np.abs(Up[I]).sum()
     assert rel < 1e-2, rel
+
+
+def test_gate_extras_repair_gives_orders_back(pkg):
+    """gpmood_set_nn_repair: a gated cell whose uniform-order update passes
+    DETECTION gets Mord back, so fewer cells start lowered; the run stays near
+    plain GP-MOOD (how near, against the gated run without the repair, depends
+    on the problem: closer on this one over 40 steps)."""
+    from gpmood_gb300 import ic, nn_train as T
+    from pathlib import Path
+    gate = Path(__file__).resolve().parents[1] / "gp-mood_gb300" / "gates" / "gate_sedov_rp2d3.txt"
+    import json
+    params = T.load_text(str(gate))
+    thr = float(json.loads(gate.with_suffix(".json").read_text())["threshold"])
+    n = 128
+    U0 = ic.rp2d3(n, n)
+
+    def run(method, repair=False):
+        with pkg.Solver(lf=n, nf=n, bc_type=17, tmax=0.8, method=method, fp_mode=pkg.FP_FAST) as s:
+            s.Boundary_C(U0, 0.0)
+            s.set_state(U0, 0.0)
+            if method == pkg.NN_GP_MOOD:
+                s.set_nn(params)
+                s.set_nn_threshold(thr)
+                s.set_nn_repair(repair)
+            prior = 0
+            for _ in range(40):
+                s.advance(1)
+                prior += s.counters().a_priori_last_step
+            U, t, _ = s.get_state()
+        return U, prior
+
+    Up, _ = run(pkg.GP_MOOD)
+    Ug, prior_g = run(pkg.NN_GP_MOOD)
+    Ur, prior_r = run(pkg.NN_GP_MOOD, repair=True)
+    assert 0 < prior_r < prior_g, (prior_r, prior_g)
+    I = (slice(4, -4), slice(4, -4), 0)
+    rel = lambda a: np.abs(a[I] - Up[I]).sum() / np.abs(Up[I]).sum()
+    assert rel(Ur) <= rel(Ug), (rel(Ur), rel(Ug))
