@@ -246,6 +246,101 @@ __device__ __forceinline__ void hllc(const double* ul, const double* ur, double*
     for (int k = 0; k < 4; k++) F[k] = Fk[k] + S * (st[k] * dStar - u[k]);
 }
 
+// The same primitive recovery, physical flux and HLLC with the direction a
+// runtime value (0: x, 1: y): every FP64 expression is the one hllc<DIR>
+// evaluates, only the choice of normal and tangential components is a select,
+// so the result has the same bits.  A warp whose lanes hold x and y faces then
+// issues each FP64 instruction once instead of once per direction.
+__device__ __forceinline__ Prim c2p_dyn(const double* u, int dir, double ir_in = 0.0) {
+    Prim s;
+#if GPM_EXACT
+    const double vx = u[1] / u[0];
+    const double vy = u[2] / u[0];
+    s.p = (GPM_GAMMA - 1.) * (u[3] - (0.5 * (u[1] * u[1] + u[2] * u[2]) / u[0]));
+    s.c = sqrt(GPM_GAMMA * s.p / u[0]);
+#else
+    const double ir = ir_in;
+    const double vx = u[1] * ir;
+    const double vy = u[2] * ir;
+    s.p = (GPM_GAMMA - 1.) * (u[3] - 0.5 * (u[1] * vx + u[2] * vy));
+    s.c = sqrt(GPM_GAMMA * s.p * ir);
+    s.ir = ir;
+#endif
+    s.vx = vx;
+    s.vn = dir == 0 ? vx : vy;
+    s.vt = dir == 0 ? vy : vx;
+    s.vn2 = s.vn * s.vn;
+    s.adm = !(le_zero_or_nan(u[0]) || le_zero_or_nan(s.p));
+    return s;
+}
+
+__device__ __forceinline__ void phys_flux_dyn(const double* u, const Prim& s, int dir, double* r) {
+    const double a = u[0] * s.vn2 + s.p;           // normal momentum flux
+    const double b = (dir == 0 ? u[2] : u[1]) * s.vn;  // tangential momentum flux
+    r[0] = dir == 0 ? u[1] : u[2];
+    r[1] = dir == 0 ? a : b;
+    r[2] = dir == 0 ? b : a;
+    r[3] = s.vn * (u[3] + s.p);
+}
+
+__device__ __forceinline__ void hllc_dyn(const double* ul, const double* ur, int dir, double* F) {
+#if GPM_EXACT
+    const Prim L = c2p_dyn(ul, dir);
+    const Prim R = c2p_dyn(ur, dir);
+#else
+    const double rr = gpm_fast_rcp(ul[0] * ur[0]);
+    const Prim L = c2p_dyn(ul, dir, ur[0] * rr);
+    const Prim R = c2p_dyn(ur, dir, ul[0] * rr);
+#endif
+    const double SL = fmin(L.vn - L.c, R.vn - R.c);
+    const double SR = fmax(L.vn + L.c, R.vn + R.c);
+    if (!(L.adm && R.adm)) {
+        const double bad = 1. / (R.vx - R.vx);
+        F[0] = F[1] = F[2] = F[3] = bad;
+        return;
+    }
+    if (SL >= 0.) {
+        phys_flux_dyn(ul, L, dir, F);
+        return;
+    }
+    const double numerL = SL - L.vn, numerR = SR - R.vn;
+    double uStar = ul[0] * L.vn * numerL - ur[0] * R.vn * numerR;
+    uStar = (R.p - L.p) + uStar;
+    const double aL = ul[0] * numerL, aR = ur[0] * numerR;
+#if GPM_EXACT
+    uStar = uStar / (aL - aR);
+#else
+    uStar = uStar * gpm_fast_rcp(aL - aR);
+#endif
+    const bool left = (SL < 0.) && (uStar >= 0.);
+    const bool right = (uStar < 0.) && (SR >= 0.);
+    if (!left && !right) {
+        phys_flux_dyn(ur, R, dir, F);
+        return;
+    }
+    const double* u = left ? ul : ur;
+    const Prim& s = left ? L : R;
+    const double S = left ? SL : SR;
+    const double a = left ? aL : aR;
+    double Fk[4];
+    phys_flux_dyn(u, s, dir, Fk);
+    double st[4];
+    st[0] = 1.;
+    st[1] = dir == 0 ? uStar : s.vt;
+    st[2] = dir == 0 ? s.vt : uStar;
+#if GPM_EXACT
+    const double dStar = a / (S - uStar);
+    st[3] = u[3] / u[0] + (uStar - s.vn) * (uStar + s.p / a);
+#else
+    const double den = S - uStar;
+    const double inv = gpm_fast_rcp(a * den);
+    const double dStar = a * a * inv;
+    st[3] = u[3] * s.ir + (uStar - s.vn) * (uStar + s.p * den * inv);
+#endif
+#pragma unroll
+    for (int k = 0; k < 4; k++) F[k] = Fk[k] + S * (st[k] * dStar - u[k]);
+}
+
 // Left/right wave-speed bounds and physical fluxes, as HLL_Flux and LLF_Flux
 // gather them (mod_HLL.f90:29-69, mod_LLF.f90:29-95); vxr is the right
 // state's x velocity for the 1/(vx-vx) of an inadmissible pair.

@@ -841,6 +841,60 @@ __device__ __forceinline__ void face_gp_any(const StageArgs& a, const GpWeights&
     f.gw = w.gw;
 }
 
+// The same face item with the direction a runtime value (0: x face between
+// c0 and c0+1, 1: y face between c0 and c0+nx): the reconstruction reads the
+// weights of the face's sides by index and HLLC runs as hllc_dyn, so a warp
+// may hold x and y faces at once; the bits are face_gp_any's.  Other Riemann
+// solvers branch on the direction.
+__device__ __forceinline__ void face_gp_dyn(const StageArgs& a, const GpWeights& w, size_t c0, int dir, int gp,
+                                            FaceGp& f) {
+    const GridGeom& g = a.g;
+    const size_t c1 = c0 + (dir == 0 ? (size_t)1 : (size_t)g.nx);
+    const int o = min((int)a.order[c0], (int)a.order[c1]);
+    const int FL = dir == 0 ? 2 : 1, FH = dir == 0 ? 0 : 3;
+    const ptrdiff_t row = g.nx;
+    double uL[4], uR[4];
+    if (o >= 5) {
+        Cell q[13];
+#pragma unroll
+        for (int m = 0; m < 13; m++) q[m] = ld_cell(a.uin + 4 * (c0 + st_ox(m) + row * st_oy(m)));
+        gp_recon_at<13>(&w.zt[2][FL][gp][0], q, uL);
+#pragma unroll
+        for (int m = 0; m < 13; m++) q[m] = ld_cell(a.uin + 4 * (c1 + st_ox(m) + row * st_oy(m)));
+        gp_recon_at<13>(&w.zt[2][FH][gp][0], q, uR);
+    } else {
+        const int NPo = o >= 3 ? 1 : 0;  // weight set: order 3 or 1
+        Cell q[5];
+#pragma unroll
+        for (int m = 0; m < 5; m++) q[m] = ld_cell(a.uin + 4 * (c0 + st_ox(m) + row * st_oy(m)));
+        if (o >= 3) gp_recon_at<5>(&w.zt[NPo][FL][gp][0], q, uL);
+        else gp_recon_at<1>(&w.zt[0][FL][gp][0], q, uL);
+        if (a.ccw) {
+            const int l0 = (int)(c0 % (size_t)g.nx) - 3, n0 = (int)(c0 / (size_t)g.nx) - 3;
+            double v1, v2;
+            cc_weights(g, a.ccw, l0, n0, &v1, &v2);
+            if (o >= 3) cc_blend<5>(v1, v2, q[0], uL);
+            else cc_blend<1>(v1, v2, q[0], uL);
+        }
+#pragma unroll
+        for (int m = 0; m < 5; m++) q[m] = ld_cell(a.uin + 4 * (c1 + st_ox(m) + row * st_oy(m)));
+        if (o >= 3) gp_recon_at<5>(&w.zt[NPo][FH][gp][0], q, uR);
+        else gp_recon_at<1>(&w.zt[0][FH][gp][0], q, uR);
+        if (a.ccw) {
+            const int l0 = (int)(c0 % (size_t)g.nx) - 3, n0 = (int)(c0 / (size_t)g.nx) - 3;
+            double v1, v2;
+            cc_weights(g, a.ccw, l0 + (dir == 0), n0 + (dir == 1), &v1, &v2);
+            if (o >= 3) cc_blend<5>(v1, v2, q[0], uR);
+            else cc_blend<1>(v1, v2, q[0], uR);
+        }
+    }
+    if (g.num_flux == 100) hllc_dyn(uL, uR, dir, f.F);
+    else if (dir == 0) riemann<0>(g.num_flux, uL, uR, f.F);
+    else riemann<1>(g.num_flux, uL, uR, f.F);
+    f.out = (dir == 0 ? a.fx : a.fy) + 4 * c0;
+    f.gw = w.gw;
+}
+
 // Faces 0 .. nf-1 dealt to whole warps (stid: pack_tid, gstride: threads of
 // the grid); item(i, gp, f) fills face i's Gauss point gp.  Faces 0 .. n0-1
 // (the x faces) and n0 .. nf-1 (the y faces) start on warp boundaries, so no
@@ -1082,11 +1136,11 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
             a.sc->detected_step += (unsigned long long)nt;
         }
         // the four faces of every troubled cell at the new orders
-        face_phase_gp<NGP>(4 * nt, 2 * nt, stid, wstride, [&](int i, int gp, FaceGp& f) {
+        // x and y faces share warps (face_gp_dyn): 4*nt items packed densely
+        face_phase_gp<NGP>(4 * nt, 4 * nt, stid, wstride, [&](int i, int gp, FaceGp& f) {
             int dir, side;
             const size_t c = (size_t)a.tlist[cur][face_item(i, nt, &dir, &side)];
-            if (dir == 0) face_gp_any<0>(a, w, side == 0 ? c - 1 : c, gp, f);
-            else face_gp_any<1>(a, w, side == 0 ? c - g.nx : c, gp, f);
+            face_gp_dyn(a, w, side == 0 ? (dir == 0 ? c - 1 : c - g.nx) : c, dir, gp, f);
         });
         if (!mood_sync(bar, solo)) return;
         // the 5-point crosses: Uout from Uin and the current fluxes, DETECTION
