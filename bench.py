@@ -55,6 +55,7 @@ def parse():
     ap.add_argument("--batch-problems", type=int, default=1024)
     ap.add_argument("--batch-steps", type=int, default=10, help="timed steps of the batched form (0: skip)")
     ap.add_argument("--adjoint", type=int, default=1, help="also time the adjoint form (0: skip)")
+    ap.add_argument("--skip-plain", type=int, default=0, help="with --final: leave out the plain run")
     ap.add_argument("--repair", type=int, default=0,
                     help="with --final: also the NN-gated run with the gate's extras repair (gpmood_set_nn_repair)")
     ap.add_argument("--l1-ref", type=int, default=0,
@@ -388,14 +389,16 @@ def run_final(args):
     variants = [("plain", pkg.GP_MOOD, False)] + ([("nn_gated", pkg.NN_GP_MOOD, False)] if args.nn else [])
     if args.nn and args.repair:
         variants.append(("nn_gated_repaired", pkg.NN_GP_MOOD, True))
+    if args.skip_plain:  # e.g. a long run whose plain half is on record already
+        variants = [v for v in variants if v[0] != "plain"]
     for name, method, repair in variants:
         out[name], finals[name] = whole_run(pkg, icname, lf, nf, lx, ly, bc, tfinal, fp, method, params, thr, repair)
         # each variant on stderr as soon as it ends, so that a long run that is cut off still reports
         print(json.dumps({"partial": name, "case": args.case, **out[name]}), file=sys.stderr, flush=True)
-    if args.nn:
+    if args.nn and "plain" in out:
         out["nn_gated"]["speedup_vs_plain"] = out["plain"]["seconds"] / out["nn_gated"]["seconds"]
         out["rel_l1_final"] = _rel_l1(finals["nn_gated"], finals["plain"])
-    if "nn_gated_repaired" in out:
+    if "nn_gated_repaired" in out and "plain" in out:
         out["nn_gated_repaired"]["speedup_vs_plain"] = out["plain"]["seconds"] / out["nn_gated_repaired"]["seconds"]
         out["nn_gated_repaired"]["rel_l1_vs_plain"] = _rel_l1(finals["nn_gated_repaired"], finals["plain"])
     if args.l1_ref:
