@@ -249,8 +249,10 @@ __device__ __forceinline__ void hllc(const double* ul, const double* ur, double*
 // The same primitive recovery, physical flux and HLLC with the direction a
 // runtime value (0: x, 1: y): every FP64 expression is the one hllc<DIR>
 // evaluates, only the choice of normal and tangential components is a select,
-// so the result has the same bits.  A warp whose lanes hold x and y faces then
-// issues each FP64 instruction once instead of once per direction.
+// so in the exact mode (no FMA contraction) the result has the same bits; in
+// the fast mode the compiler's contraction may differ at rounding level.  A
+// warp whose lanes hold x and y faces then issues each FP64 instruction once
+// instead of once per direction.
 __device__ __forceinline__ Prim c2p_dyn(const double* u, int dir, double ir_in = 0.0) {
     Prim s;
 #if GPM_EXACT

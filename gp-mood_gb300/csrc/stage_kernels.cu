@@ -844,8 +844,8 @@ __device__ __forceinline__ void face_gp_any(const StageArgs& a, const GpWeights&
 // The same face item with the direction a runtime value (0: x face between
 // c0 and c0+1, 1: y face between c0 and c0+nx): the reconstruction reads the
 // weights of the face's sides by index and HLLC runs as hllc_dyn, so a warp
-// may hold x and y faces at once; the bits are face_gp_any's.  Other Riemann
-// solvers branch on the direction.
+// may hold x and y faces at once; in the exact mode the bits are
+// face_gp_any's.  Other Riemann solvers branch on the direction.
 __device__ __forceinline__ void face_gp_dyn(const StageArgs& a, const GpWeights& w, size_t c0, int dir, int gp,
                                             FaceGp& f) {
     const GridGeom& g = a.g;
