@@ -1046,36 +1046,64 @@ __device__ __forceinline__ bool mood_sync(GridBar* b, bool solo) {
 // two U2 tests; after a CTA barrier role 0 combines them, lowers the order of
 // a troubled cell and lists it.  The decision is mood_troubled's.
 constexpr int SOLO_CHUNK = MOOD_THREADS / 4;  // cross cells per chunk (one per lane of each role)
+// One-CTA passes keep the troubled lists in shared memory (every entry is also
+// written to the global list, which a list longer than this is read from):
+// reading a list entry and appending one then costs the SM's shared-memory
+// latency instead of an L2 round trip or a global atomic.
+constexpr int SOLO_LIST_CAP = 2048;
 
 struct SoloCross {
     int cell[SOLO_CHUNK];
     int8_t part[SOLO_CHUNK];      // mood_uout_part; -1: ghost cell or already updated in this pass
+    int8_t ord[SOLO_CHUNK];       // the cell's order when it was checked
     bool flag[3][SOLO_CHUNK];     // shock, U2 smooth in x, U2 smooth in y
 };
 
+struct SoloLists {
+    int list[2][SOLO_LIST_CAP];
+    int count[2];
+};
+
+// lst: the current troubled list (shared or global), nt entries.  A cross
+// cell that several listed cells share is updated once: in a pass that fits
+// one chunk by the first listed cell whose cross holds it (a scan of the
+// shared list), otherwise by whoever stamps it first (global atomics).
 __device__ __forceinline__ void solo_cross(const StageArgs& a, const GpWeights& w, int cur, int nt, unsigned pid,
-                                           SoloCross& sm) {
+                                           const int* lst, SoloCross& sm, SoloLists& sl) {
     const GridGeom& g = a.g;
     const double qx = a.sc->qx, qy = a.sc->qy;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int role = warp & 3, j = (warp >> 2) * 32 + lane;  // item of the chunk
     const int nxt = cur ^ 1, total = 5 * nt;
+    const bool scan = total <= SOLO_CHUNK && nt <= SOLO_LIST_CAP;  // one chunk, list in shared memory
+    const int nx = g.nx;
     for (int base = 0; base < total; base += SOLO_CHUNK) {
         const int i = base + j;
         if (i < total) {
-            const size_t t = (size_t)a.tlist[cur][i / 5];
+            const int q = i / 5;
+            const size_t t = (size_t)lst[q];
             const int k = i % 5;
-            const size_t c = k == 0 ? t - g.nx : k == 1 ? t - 1 : k == 2 ? t : k == 3 ? t + 1 : t + g.nx;
-            const int l = (int)(c % (size_t)g.nx) - 3, n = (int)(c / (size_t)g.nx) - 3;
+            const size_t c = k == 0 ? t - nx : k == 1 ? t - 1 : k == 2 ? t : k == 3 ? t + 1 : t + nx;
+            const int l = (int)(c % (size_t)nx) - 3, n = (int)(c / (size_t)nx) - 3;
             const bool interior = l >= 1 && l <= g.lf && n >= 1 && n <= g.nf;
             const double* uin = a.uin + 4 * c;
             if (role == 0) {
-                int r = -1;
-                if (interior && atomicExch(&a.stamp[c], pid) != pid) {
+                bool own = interior;
+                if (own && scan) {
+                    for (int q2 = 0; q2 < q; q2++) {
+                        const long long d = (long long)c - (long long)lst[q2];
+                        if (d == 0 || d == 1 || d == -1 || d == nx || d == -nx) own = false;
+                    }
+                } else if (own) {
+                    own = atomicExch(&a.stamp[c], pid) != pid;
+                }
+                int r = -1, o = 0;
+                if (own) {
                     const Cell uo = cell_update(g, a.uin, a.fx, a.fy, c, qx, qy);
                     st_cell(a.uout + 4 * c, uo);
-                    if (a.order[c] > 1) {
-                        r = mood_uout_part(uo, uin, g.nx, g);
+                    o = a.order[c];
+                    if (o > 1) {
+                        r = mood_uout_part(uo, uin, nx, g);
                     } else {
                         if (inadmissible(uo)) atomicOr(&a.sc->status, GPM_STATUS_NAN);
                         r = 0;
@@ -1083,10 +1111,11 @@ __device__ __forceinline__ void solo_cross(const StageArgs& a, const GpWeights& 
                 }
                 sm.cell[j] = (int)c;
                 sm.part[j] = (int8_t)r;
+                sm.ord[j] = (int8_t)o;
             } else if (interior) {
-                sm.flag[role - 1][j] = role == 1   ? mood_shock_part(uin, g.nx, g)
-                                       : role == 2 ? mood_u2_smooth<0>(uin, g.nx, g, w.d2x)
-                                                   : mood_u2_smooth<1>(uin, g.nx, g, w.d2y);
+                sm.flag[role - 1][j] = role == 1   ? mood_shock_part(uin, nx, g)
+                                       : role == 2 ? mood_u2_smooth<0>(uin, nx, g, w.d2x)
+                                                   : mood_u2_smooth<1>(uin, nx, g, w.d2y);
             }
         }
         __syncthreads();
@@ -1098,8 +1127,22 @@ __device__ __forceinline__ void solo_cross(const StageArgs& a, const GpWeights& 
                 cval = sm.cell[j];
                 trb = r == 1 || (r == 2 && sm.flag[0][j] && !(g.u2 && (sm.flag[1][j] || sm.flag[2][j])));
             }
-            if (trb) cascade_order(&a.order[cval]);
-            list_append(trb, a.tlist[nxt], &a.sc->ntrb[nxt], cval);
+            if (trb) {  // the cascade of cascade_order, on the order read above
+                const int v = sm.ord[j];
+                a.order[cval] = (int8_t)(v == 3 ? 1 : (v > 3 ? 3 : v));
+            }
+            // warp-aggregated append to the next list, shared and global
+            const unsigned m = __ballot_sync(0xffffffffu, trb);
+            if (m) {
+                int b0 = 0;
+                if (lane == 0) b0 = atomicAdd(&sl.count[nxt], __popc(m));
+                b0 = __shfl_sync(0xffffffffu, b0, 0);
+                if (trb) {
+                    const int idx = b0 + __popc(m & ((1u << lane) - 1));
+                    a.tlist[nxt][idx] = cval;
+                    if (idx < SOLO_LIST_CAP) sl.list[nxt][idx] = cval;
+                }
+            }
         }
         __syncthreads();
     }
@@ -1109,15 +1152,16 @@ template <int NGP>
 __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, const __grid_constant__ GpWeights w, GridBar* bar,
                                                       int max_pass, int stage) {
     __shared__ SoloCross solo_sm;
+    __shared__ SoloLists solo_ls;
     const GridGeom& g = a.g;
     const double qx = a.sc->qx, qy = a.sc->qy;
     const unsigned epoch = a.sc->stamp_epoch;  // stamps epoch+2, epoch+3, ... are new
     const int gtid = blockIdx.x * blockDim.x + threadIdx.x, gstride = gridDim.x * blockDim.x;
     int stid = pack_tid(), wstride = gstride;  // whole warps of work items, dealt over all SMs
-    bool solo = false;
+    bool solo = false, shared_lists = false;  // shared_lists: a one-CTA loop with role-split DETECTION
     int cur = 0, pass = 1;  // pass 1 (all faces) ran before this kernel
     for (;;) {
-        const int nt = *(volatile int*)&a.sc->ntrb[cur];
+        const int nt = shared_lists ? solo_ls.count[cur] : *(volatile int*)&a.sc->ntrb[cur];
         if (nt == 0) break;
         if (pass >= max_pass) {
             if (gtid == 0) a.sc->status |= GPM_STATUS_MOODCAP;
@@ -1128,25 +1172,34 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
             solo = true;
             stid = threadIdx.x;
             wstride = blockDim.x;
+            if (g.solo_split) {  // from here on the lists also live in shared memory
+                shared_lists = true;
+                for (int i = threadIdx.x; i < nt && i < SOLO_LIST_CAP; i += blockDim.x)
+                    solo_ls.list[cur][i] = a.tlist[cur][i];
+                if (threadIdx.x == 0) solo_ls.count[cur] = nt;
+                __syncthreads();
+            }
         }
         pass++;
         // the listed cells' orders were lowered when they were listed
         if (gtid == 0) {
             a.sc->ntrb[cur ^ 1] = 0;  // nobody appends to it before the next barrier
             a.sc->detected_step += (unsigned long long)nt;
+            if (shared_lists) solo_ls.count[cur ^ 1] = 0;
         }
+        const int* lst = shared_lists && nt <= SOLO_LIST_CAP ? solo_ls.list[cur] : a.tlist[cur];
         // the four faces of every troubled cell at the new orders
         // x and y faces share warps (face_gp_dyn): 4*nt items packed densely
         face_phase_gp<NGP>(4 * nt, 4 * nt, stid, wstride, [&](int i, int gp, FaceGp& f) {
             int dir, side;
-            const size_t c = (size_t)a.tlist[cur][face_item(i, nt, &dir, &side)];
+            const size_t c = (size_t)lst[face_item(i, nt, &dir, &side)];
             face_gp_dyn(a, w, side == 0 ? (dir == 0 ? c - 1 : c - g.nx) : c, dir, gp, f);
         });
         if (!mood_sync(bar, solo)) return;
         // the 5-point crosses: Uout from Uin and the current fluxes, DETECTION
         const unsigned pid = epoch + (unsigned)pass;
-        if (solo && g.solo_split) {
-            solo_cross(a, w, cur, nt, pid, solo_sm);
+        if (shared_lists) {
+            solo_cross(a, w, cur, nt, pid, lst, solo_sm, solo_ls);
             cur ^= 1;
             continue;
         }
@@ -1178,6 +1231,7 @@ __global__ void __launch_bounds__(MOOD_THREADS, 1) k_mood_loop(StageArgs a, cons
     if (gtid == 0) {  // every CTA read the epoch before the first barrier
         a.sc->passes_stage[stage] = pass;
         a.sc->stamp_epoch = epoch + (unsigned)pass + 1u;
+        if (shared_lists) a.sc->ntrb[cur] = solo_ls.count[cur];
     }
 }
 
