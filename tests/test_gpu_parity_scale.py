@@ -7,8 +7,9 @@
   10 steps from t = 0 through the device-resident loop: 1e-12 and identical
   masks against the oracle (OpenMP on the host cores).
 * Whole runs to t_final (the main.f90:145-203 loop) on the shock problems:
-  2DRP3 128^2 to 0.8, Sedov 128^2 to 0.05, DMR 256x64 to 0.2.  Exact mode bit
-  for bit; fast mode within 1e-8 relative L1 per field.
+  2DRP3 128^2 and 256^2 (the CPU-runnable configuration) to 0.8, Sedov 128^2
+  and 256^2 to 0.05, DMR 256x64 to 0.2.  Exact mode bit for bit; fast mode
+  within 1e-8 relative L1 per field.
 * The per-step counters (count_detected_cell of mod_subroutine_MOOD.f90:153,
   printed as a percentage at main.f90:165-167, and the MOOD pass counts)
   against the oracle's.
@@ -29,6 +30,9 @@ WHOLE = {
     "rp2d3_128": ("rp2d3", 128, 128, 17, 1.0, 1.0, 0.8),
     "sedov_128": ("sedov", 128, 128, 20, 1.0, 1.0, 0.05),
     "dmr_256x64": ("dmr", 256, 64, 35, 4.0, 1.0, 0.2),
+    # the CPU-runnable benchmark configuration itself, and Sedov at the same size
+    "rp2d3_256": ("rp2d3", 256, 256, 17, 1.0, 1.0, 0.8),
+    "sedov_256": ("sedov", 256, 256, 20, 1.0, 1.0, 0.05),
 }
 
 
