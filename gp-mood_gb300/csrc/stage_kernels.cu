@@ -571,7 +571,7 @@ static PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 }
 
 // The tile map of a padded state: ny rows of 4*nx doubles, boxes of XY+5 rows
-// by 4*(XT+5) doubles.  False if the driver refuses it or the state is not
+// by 4*(XT+5) doubles.  False if the CUDA driver refuses it or the state is not
 // 16-byte aligned (TMA's rule for the global address).
 static bool encode_tile_map(CUtensorMap* m, const double* u, const GridGeom& g) {
     PFN_cuTensorMapEncodeTiled_v12000 enc = tensor_map_encoder();
