@@ -488,20 +488,28 @@ __device__ __forceinline__ void quad_flux(const double (*uL)[4], const double (*
 #endif
 }
 
-// shock_detector, mod_subroutine_MOOD.f90:191-238, on Uin around (l, n).
+// shock_detector, mod_subroutine_MOOD.f90:191-238, on Uin around (l, n), in
+// two side-effect-free halves that the MOOD loop may evaluate on different
+// warps: shock_flow, the compressive-flow tests divV < -max(dx,dy)^2 and
+// Mach > 0.2, and shock_grad, the pressure-jump test gradP > 5.
 #if GPM_EXACT
-__device__ __forceinline__ bool shock_detector(const Cell& c, const Cell& L, const Cell& R, const Cell& B,
-                                               const Cell& T, double dx, double dy) {
+__device__ __forceinline__ bool shock_flow(const Cell& c, const Cell& L, const Cell& R, const Cell& B,
+                                           const Cell& T, double dx, double dy) {
     double divV = (R.mx - L.mx) / dx + (T.my - B.my) / dy;
     divV = 0.5 * divV / c.r;
     divV = divV - 0.5 * (c.mx * (R.r - L.r) / dx + c.my * (T.r - B.r) / dy) / (c.r * c.r);
     const double Ca = 1.4 * pressure(c) / c.r;
     double Mach = (c.mx * c.mx + c.my * c.my) / (c.r * c.r);
     Mach = sqrt(Mach / Ca);
+    const double m = fmax(dx, dy);
+    return (divV < -(m * m)) && (Mach > 0.2);
+}
+
+__device__ __forceinline__ bool shock_grad(const Cell& L, const Cell& R, const Cell& B, const Cell& T, double dx,
+                                           double dy) {
     const double pL = pressure(L), pR = pressure(R), pB = pressure(B), pT = pressure(T);
     const double gradP = 0.5 * (fabs(pR - pL) / fmin(pL, pR) / dx + fabs(pT - pB) / fmin(pB, pT) / dy);
-    const double m = fmax(dx, dy);
-    return (divV < -(m * m)) && (Mach > 0.2) && (gradP > 5.0);
+    return gradP > 5.0;
 }
 #else
 // Fast mode: p with a supplied 1/rho.
@@ -513,8 +521,8 @@ __device__ __forceinline__ double pressure_ir(const Cell& u, double ir) {
 // in place of the nineteen IEEE divisions; the quantities agree with the
 // exact form to rounding for admissible states.  A lone warp pays ~64 cycles
 // per FP64 instruction, and a short MOOD pass waits on this chain.
-__device__ __forceinline__ bool shock_detector(const Cell& c, const Cell& L, const Cell& R, const Cell& B,
-                                               const Cell& T, double dx, double dy) {
+__device__ __forceinline__ bool shock_flow(const Cell& c, const Cell& L, const Cell& R, const Cell& B,
+                                           const Cell& T, double dx, double dy) {
     const double ixy = gpm_fast_rcp(dx * dy);
     const double idx = dy * ixy, idy = dx * ixy;
     const double ir = gpm_fast_rcp(c.r), ir2 = ir * ir;
@@ -523,15 +531,27 @@ __device__ __forceinline__ bool shock_detector(const Cell& c, const Cell& L, con
     divV = divV - 0.5 * (c.mx * (R.r - L.r) * idx + c.my * (T.r - B.r) * idy) * ir2;
     const double Ca = 1.4 * pressure_ir(c, ir) * ir;
     const double Mach = sqrt((c.mx * c.mx + c.my * c.my) * ir2 * gpm_fast_rcp(Ca));
+    const double m = fmax(dx, dy);
+    return (divV < -(m * m)) && (Mach > 0.2);
+}
+
+__device__ __forceinline__ bool shock_grad(const Cell& L, const Cell& R, const Cell& B, const Cell& T, double dx,
+                                           double dy) {
+    const double ixy = gpm_fast_rcp(dx * dy);
+    const double idx = dy * ixy, idy = dx * ixy;
     const double rlr = gpm_fast_rcp(L.r * R.r), rbt = gpm_fast_rcp(B.r * T.r);
     const double pL = pressure_ir(L, R.r * rlr), pR = pressure_ir(R, L.r * rlr);
     const double pB = pressure_ir(B, T.r * rbt), pT = pressure_ir(T, B.r * rbt);
     const double gradP = 0.5 * (fabs(pR - pL) * gpm_fast_rcp(fmin(pL, pR)) * idx +
                                 fabs(pT - pB) * gpm_fast_rcp(fmin(pB, pT)) * idy);
-    const double m = fmax(dx, dy);
-    return (divV < -(m * m)) && (Mach > 0.2) && (gradP > 5.0);
+    return gradP > 5.0;
 }
 #endif
+
+__device__ __forceinline__ bool shock_detector(const Cell& c, const Cell& L, const Cell& R, const Cell& B,
+                                               const Cell& T, double dx, double dy) {
+    return shock_flow(c, L, R, B, T, dx, dy) && shock_grad(L, R, B, T, dx, dy);
+}
 
 // An order-1 cell is never checked again (mod_subroutine_MOOD.f90:41), so a
 // NaN or non-positive density or pressure in it survives the stage; callers
@@ -583,6 +603,21 @@ __device__ __forceinline__ bool mood_shock_part(const double* __restrict__ uin, 
     const Cell C = ld_cell(uin), Lc = ld_cell(uin - 4), Rc = ld_cell(uin + 4);
     const Cell Bc = ld_cell(uin - row), Tc = ld_cell(uin + row);
     return shock_detector(C, Lc, Rc, Bc, Tc, g.dx, g.dy);
+}
+
+// The shock detector's two halves on their own, for warps that run one each.
+__device__ __forceinline__ bool mood_shock_flow_part(const double* __restrict__ uin, int nx, const GridGeom& g) {
+    const size_t row = (size_t)4 * nx;
+    const Cell C = ld_cell(uin), Lc = ld_cell(uin - 4), Rc = ld_cell(uin + 4);
+    const Cell Bc = ld_cell(uin - row), Tc = ld_cell(uin + row);
+    return shock_flow(C, Lc, Rc, Bc, Tc, g.dx, g.dy);
+}
+
+__device__ __forceinline__ bool mood_shock_grad_part(const double* __restrict__ uin, int nx, const GridGeom& g) {
+    const size_t row = (size_t)4 * nx;
+    const Cell Lc = ld_cell(uin - 4), Rc = ld_cell(uin + 4);
+    const Cell Bc = ld_cell(uin - row), Tc = ld_cell(uin + row);
+    return shock_grad(Lc, Rc, Bc, Tc, g.dx, g.dy);
 }
 
 // DIR 0: the x test on D2x, 1: the y test on D2y.

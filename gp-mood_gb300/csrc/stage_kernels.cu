@@ -1040,12 +1040,15 @@ __device__ __forceinline__ bool mood_sync(GridBar* b, bool solo) {
 // The cross phase of a pass run by one CTA (solo).  A lone warp pays ~64
 // cycles for every FP64 instruction, so one cross cell's DETECTION chain
 // (update, positivity, DMP bounds, shock detector, U2 in x and in y) is what
-// a short pass waits on.  Its parts are split over four warp roles that run
+// a short pass waits on.  Its parts are split over five warp roles that run
 // at once on every cross cell of a chunk: role 0 updates Uout and runs the
-// Uout tests (mood_uout_part), roles 1-3 the Uin-only shock detector and the
-// two U2 tests; after a CTA barrier role 0 combines them, lowers the order of
-// a troubled cell and lists it.  The decision is mood_troubled's.
-constexpr int SOLO_CHUNK = MOOD_THREADS / 4;  // cross cells per chunk (one per lane of each role)
+// Uout tests (mood_uout_part), roles 1-4 the Uin-only tests -- the shock
+// detector's flow half, the two U2 tests and the shock detector's
+// pressure-jump half; after a CTA barrier role 0 combines them, lowers the
+// order of a troubled cell and lists it.  The decision is mood_troubled's.
+// Warp w takes role w % 5; 16 warps give every role at least 3 warps.
+constexpr int SOLO_ROLES = 5;
+constexpr int SOLO_CHUNK = (MOOD_THREADS / 32 / SOLO_ROLES) * 32;  // cross cells per chunk (96)
 // One-CTA passes keep the troubled lists in shared memory (every entry is also
 // written to the global list, which a list longer than this is read from):
 // reading a list entry and appending one then costs the SM's shared-memory
@@ -1056,7 +1059,7 @@ struct SoloCross {
     int cell[SOLO_CHUNK];
     int8_t part[SOLO_CHUNK];      // mood_uout_part; -1: ghost cell or already updated in this pass
     int8_t ord[SOLO_CHUNK];       // the cell's order when it was checked
-    bool flag[3][SOLO_CHUNK];     // shock, U2 smooth in x, U2 smooth in y
+    bool flag[4][SOLO_CHUNK];     // shock flow half, U2 smooth in x, U2 smooth in y, shock pressure-jump half
 };
 
 struct SoloLists {
@@ -1073,13 +1076,14 @@ __device__ __forceinline__ void solo_cross(const StageArgs& a, const GpWeights& 
     const GridGeom& g = a.g;
     const double qx = a.sc->qx, qy = a.sc->qy;
     const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int role = warp & 3, j = (warp >> 2) * 32 + lane;  // item of the chunk
+    const int role = warp % SOLO_ROLES, j = (warp / SOLO_ROLES) * 32 + lane;  // item of the chunk
+    const bool slot = j < SOLO_CHUNK;  // a role's fourth warp (warp 15) has no items
     const int nxt = cur ^ 1, total = 5 * nt;
     const bool scan = total <= SOLO_CHUNK && nt <= SOLO_LIST_CAP;  // one chunk, list in shared memory
     const int nx = g.nx;
     for (int base = 0; base < total; base += SOLO_CHUNK) {
         const int i = base + j;
-        if (i < total) {
+        if (slot && i < total) {
             const int q = i / 5;
             const size_t t = (size_t)lst[q];
             const int k = i % 5;
@@ -1113,19 +1117,21 @@ __device__ __forceinline__ void solo_cross(const StageArgs& a, const GpWeights& 
                 sm.part[j] = (int8_t)r;
                 sm.ord[j] = (int8_t)o;
             } else if (interior) {
-                sm.flag[role - 1][j] = role == 1   ? mood_shock_part(uin, nx, g)
+                sm.flag[role - 1][j] = role == 1   ? mood_shock_flow_part(uin, nx, g)
                                        : role == 2 ? mood_u2_smooth<0>(uin, nx, g, w.d2x)
-                                                   : mood_u2_smooth<1>(uin, nx, g, w.d2y);
+                                       : role == 3 ? mood_u2_smooth<1>(uin, nx, g, w.d2y)
+                                                   : mood_shock_grad_part(uin, nx, g);
             }
         }
         __syncthreads();
         if (role == 0) {
             bool trb = false;
             int cval = 0;
-            if (i < total && sm.part[j] >= 0) {
+            if (slot && i < total && sm.part[j] >= 0) {
                 const int r = sm.part[j];
                 cval = sm.cell[j];
-                trb = r == 1 || (r == 2 && sm.flag[0][j] && !(g.u2 && (sm.flag[1][j] || sm.flag[2][j])));
+                const bool shock = sm.flag[0][j] && sm.flag[3][j];
+                trb = r == 1 || (r == 2 && shock && !(g.u2 && (sm.flag[1][j] || sm.flag[2][j])));
             }
             if (trb) {  // the cascade of cascade_order, on the order read above
                 const int v = sm.ord[j];
