@@ -512,7 +512,7 @@ def run_ours(args, ws, rank, local):
 
     pkg = ge.import_package()
     from gpmood_gb300 import ic
-    from gpmood_gb300.gpmood import probe_fp64
+    from gpmood_gb300.gpmood import probe_fp64, probe_fp64_pipes
 
     torch.cuda.set_device(local)
     n, K, W = args.n, args.steps, max(args.warmup, 3)
@@ -522,6 +522,7 @@ def run_ours(args, ws, rank, local):
     solver.Boundary_C(U0, 0.0)
     state_bytes = U0.nbytes
     peak_fp64_gflops = probe_fp64()
+    fp64_pipes = probe_fp64_pipes()
 
     def barrier():
         dist_barrier(ws)
@@ -657,6 +658,7 @@ def run_ours(args, ws, rank, local):
         "roofline": roofline, "roofline_hbm": roofline_hbm, "cpu_baseline": cpu, "e2e": e2e,
         "gpu_launches": launches, "clocks": clk,
         "fp64_peak_gflops": peak_fp64_gflops,
+        "fp64_pipes_gflops": fp64_pipes,
         "flops_per_cell_update": FLOPS_PER_CELL_UPDATE,
         "achieved_step_tflops": FLOPS_PER_CELL_UPDATE * value / ws / 1e12,
         "mood_share_of_step": tm.mood_ms / el_ms if el_ms else None,

@@ -64,8 +64,10 @@ struct gpmood_ctx {
 };
 
 double gpm_probe_fp64();
+int gpm_probe_fp64_pipes(double* gflops);
 extern "C" void gpm_pol_weights(GpWeights* w);
 int gpm_fast_rcp_dev(const double* x, double* y, int n);
+int gpm_fast_sqrt_dev(const double* x, double* y, int n);
 
 int gpm_mood_solo_default() {
     static const int v = [] {
@@ -861,9 +863,22 @@ int gpmood_probe_fp64(double* gflops) {
     return 0;
 }
 
+int gpmood_probe_fp64_pipes(double* gflops3) {
+    if (!gflops3) return fail(nullptr, GPMOOD_E_ARG, "NULL argument");
+    if (gpm_probe_fp64_pipes(gflops3))
+        return fail(nullptr, GPMOOD_E_CUDA, "FP64 pipe probe failed: %s", cudaGetErrorString(cudaGetLastError()));
+    return 0;
+}
+
 int gpmood_fast_rcp(const double* d_x, double* d_y, int n) {
     if ((!d_x || !d_y) && n > 0) return fail(nullptr, GPMOOD_E_ARG, "NULL argument");
     if (gpm_fast_rcp_dev(d_x, d_y, n)) return fail(nullptr, GPMOOD_E_CUDA, "fast_rcp: %s", cudaGetErrorString(cudaGetLastError()));
+    return 0;
+}
+
+int gpmood_fast_sqrt(const double* d_x, double* d_y, int n) {
+    if ((!d_x || !d_y) && n > 0) return fail(nullptr, GPMOOD_E_ARG, "NULL argument");
+    if (gpm_fast_sqrt_dev(d_x, d_y, n)) return fail(nullptr, GPMOOD_E_CUDA, "fast_sqrt: %s", cudaGetErrorString(cudaGetLastError()));
     return 0;
 }
 

@@ -134,9 +134,10 @@ __device__ __forceinline__ void gp_recon_sym3(const GpSym& c, const Cell* q, dou
 #endif
 
 // Primitive recovery of one face state, c2p_local (physics.f90:51-75): normal
-// velocity vn, tangential velocity vt, vn^2, pressure, sound speed, admissibility.
+// velocity vn, tangential velocity vt, pressure, sound speed, admissibility
+// (vn^2 is formed by the one physical flux that needs it).
 struct Prim {
-    double vn, vt, vn2, p, c;
+    double vn, vt, p, c;
     bool adm;
     double vx;  // x-velocity, needed for the 1/(vx-vx) of an inadmissible state
 #if !GPM_EXACT
@@ -157,13 +158,12 @@ __device__ __forceinline__ Prim c2p(const double* u, double ir_in = 0.0) {
     const double vx = u[1] * ir;
     const double vy = u[2] * ir;
     s.p = (GPM_GAMMA - 1.) * (u[3] - 0.5 * (u[1] * vx + u[2] * vy));
-    s.c = sqrt(GPM_GAMMA * s.p * ir);
+    s.c = gpm_fast_sqrt(GPM_GAMMA * s.p * ir);  // NaN for p <= 0, which is inadmissible
     s.ir = ir;
 #endif
     s.vx = vx;
     s.vn = DIR == 0 ? vx : vy;
     s.vt = DIR == 0 ? vy : vx;
-    s.vn2 = s.vn * s.vn;
     s.adm = !(le_zero_or_nan(u[0]) || le_zero_or_nan(s.p));
     return s;
 }
@@ -173,13 +173,13 @@ template <int DIR>
 __device__ __forceinline__ void phys_flux(const double* u, const Prim& s, double* r) {
     if (DIR == 0) {
         r[0] = u[1];
-        r[1] = u[0] * s.vn2 + s.p;
+        r[1] = u[0] * (s.vn * s.vn) + s.p;
         r[2] = u[2] * s.vn;
         r[3] = s.vn * (u[3] + s.p);
     } else {
         r[0] = u[2];
         r[1] = u[1] * s.vn;
-        r[2] = u[0] * s.vn2 + s.p;
+        r[2] = u[0] * (s.vn * s.vn) + s.p;
         r[3] = s.vn * (u[3] + s.p);
     }
 }
@@ -265,19 +265,18 @@ __device__ __forceinline__ Prim c2p_dyn(const double* u, int dir, double ir_in =
     const double vx = u[1] * ir;
     const double vy = u[2] * ir;
     s.p = (GPM_GAMMA - 1.) * (u[3] - 0.5 * (u[1] * vx + u[2] * vy));
-    s.c = sqrt(GPM_GAMMA * s.p * ir);
+    s.c = gpm_fast_sqrt(GPM_GAMMA * s.p * ir);  // NaN for p <= 0, which is inadmissible
     s.ir = ir;
 #endif
     s.vx = vx;
     s.vn = dir == 0 ? vx : vy;
     s.vt = dir == 0 ? vy : vx;
-    s.vn2 = s.vn * s.vn;
     s.adm = !(le_zero_or_nan(u[0]) || le_zero_or_nan(s.p));
     return s;
 }
 
 __device__ __forceinline__ void phys_flux_dyn(const double* u, const Prim& s, int dir, double* r) {
-    const double a = u[0] * s.vn2 + s.p;           // normal momentum flux
+    const double a = u[0] * (s.vn * s.vn) + s.p;   // normal momentum flux
     const double b = (dir == 0 ? u[2] : u[1]) * s.vn;  // tangential momentum flux
     r[0] = dir == 0 ? u[1] : u[2];
     r[1] = dir == 0 ? a : b;
@@ -530,7 +529,7 @@ __device__ __forceinline__ bool shock_flow(const Cell& c, const Cell& L, const C
     divV = 0.5 * divV * ir;
     divV = divV - 0.5 * (c.mx * (R.r - L.r) * idx + c.my * (T.r - B.r) * idy) * ir2;
     const double Ca = 1.4 * pressure_ir(c, ir) * ir;
-    const double Mach = sqrt((c.mx * c.mx + c.my * c.my) * ir2 * gpm_fast_rcp(Ca));
+    const double Mach = gpm_fast_sqrt((c.mx * c.mx + c.my * c.my) * ir2 * gpm_fast_rcp(Ca));  // NaN at rest: not > 0.2
     const double m = fmax(dx, dy);
     return (divV < -(m * m)) && (Mach > 0.2);
 }

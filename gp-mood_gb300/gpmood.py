@@ -101,7 +101,9 @@ SIGNATURES = {
     "gpmood_set_timing": ([C.c_void_p, C.c_int], C.c_int),
     "gpmood_get_timing": ([C.c_void_p, C.POINTER(Timing)], C.c_int),
     "gpmood_probe_fp64": ([_DP], C.c_int),
+    "gpmood_probe_fp64_pipes": ([_DP], C.c_int),
     "gpmood_fast_rcp": ([C.c_void_p, C.c_void_p, C.c_int], C.c_int),
+    "gpmood_fast_sqrt": ([C.c_void_p, C.c_void_p, C.c_int], C.c_int),
     "gpmood_time_stepping_noalloc": ([C.POINTER(Params), C.c_void_p, C.c_void_p, C.c_double, C.c_double,
                                       C.c_void_p, C.POINTER(C.c_int)], C.c_int),
     "gpmood_batch_create": ([C.POINTER(Params), C.c_int, C.POINTER(C.c_int), C.POINTER(C.c_int),
@@ -184,6 +186,19 @@ def probe_fp64() -> float:
         L.gpmood_last_error(None, buf, 512)
         raise GpmoodError(rc, buf.value.decode(errors="replace"))
     return g.value
+
+
+def probe_fp64_pipes() -> dict:
+    """GFLOP/s of FP64 FMA chains alone, FP64 m8n8k4 MMAs alone, and both at
+    once (half the warps each): whether the tensor-core path adds FP64 rate."""
+    g = (C.c_double * 3)()
+    L = load_library()
+    rc = L.gpmood_probe_fp64_pipes(g)
+    if rc != 0:
+        buf = C.create_string_buffer(512)
+        L.gpmood_last_error(None, buf, 512)
+        raise GpmoodError(rc, buf.value.decode(errors="replace"))
+    return {"dfma": g[0], "dmma": g[1], "mixed": g[2]}
 
 
 @dataclass

@@ -275,9 +275,18 @@ int  gpmood_get_timing(const gpmood_ctx* ctx, gpmood_timing* out);
 /* FP64 FMA throughput of the current GPU in GFLOP/s (2 flops per FMA),
  * from a short dependent-chain microbenchmark; the FP64 roofline denominator. */
 int  gpmood_probe_fp64(double* gflops);
+/* Whether FP64 mma.sync adds to the FMA pipe: gflops3[0..2] = GFLOP/s of FMA
+ * chains alone, m8n8k4 FP64 MMAs alone, and half the warps on each with equal
+ * flops per half.  A mixed rate near the single ones means that the two share
+ * the FP64 hardware.  Measurement only; no reference counterpart. */
+int  gpmood_probe_fp64_pipes(double* gflops3);
 /* The fast mode's reciprocal (Newton-Raphson from the hardware approximation)
  * on device arrays: d_y[i] = 1/d_x[i]; for testing its accuracy. */
 int  gpmood_fast_rcp(const double* d_x, double* d_y, int n);
+/* The fast mode's square root (from the hardware's approximate reciprocal
+ * square root, one coupled Newton step and a final correction) on device
+ * arrays: d_y[i] = sqrt(d_x[i]); for testing its accuracy. */
+int  gpmood_fast_sqrt(const double* d_x, double* d_y, int n);
 
 /* ---- a-priori MLP gate (method GPMOOD_NN_GP_MOOD) ---- */
 
