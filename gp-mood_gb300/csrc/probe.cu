@@ -110,13 +110,13 @@ double gpm_probe_fp64() {
 
 // Whether FP64 mma.sync (DMMA) adds to the DFMA pipe: gflops[0..2] = GFLOP/s of
 // DFMA alone, DMMA alone, and half the warps on each (equal flops per half),
-// best of three after a warm-up, 4 CTAs of 256 threads per SM.  A mixed rate
+// best of three after a warm-up, 8 CTAs of 256 threads per SM (as the FMA probe).  A mixed rate
 // near the single ones means the two share the FP64 hardware.  0 or -1.
 int gpm_probe_fp64_pipes(double* gflops) {
     int dev = 0, sms = 0;
     if (cudaGetDevice(&dev) != cudaSuccess) return -1;
     if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return -1;
-    const int blocks = sms * 4, threads = 256, iters_m = 1000, iters_f = 4000;
+    const int blocks = sms * 8, threads = 256, iters_m = 500, iters_f = 2000;
     double* out = nullptr;
     if (cudaMalloc(&out, sizeof(double) * blocks * threads) != cudaSuccess) return -1;
     cudaEvent_t e0, e1;
