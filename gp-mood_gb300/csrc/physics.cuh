@@ -578,14 +578,11 @@ __device__ __forceinline__ bool inadmissible(const Cell& uo) {
 // effect free, so evaluating them in any order, or all of them, gives the
 // reference's decision.  uin points at Uin(1, l, n) of a padded array of row
 // pitch 4*nx doubles.
+#if GPM_EXACT
 __device__ __forceinline__ int mood_uout_part(const Cell& uo, const double* __restrict__ uin, int nx,
                                               const GridGeom& g) {
     if (le_zero_or_nan(uo.r)) return 1;
-#if GPM_EXACT
     const double p = pressure(uo);
-#else
-    const double p = pressure_ir(uo, gpm_fast_rcp(uo.r));
-#endif
     if (le_zero_or_nan(p)) return 1;
     if (!g.dmp) return 0;
     const size_t row = (size_t)4 * nx;
@@ -596,6 +593,41 @@ __device__ __forceinline__ int mood_uout_part(const Cell& uo, const double* __re
     if (!(Mm > g.dx * g.dx * g.dx)) return 0;          // plateau, :68
     return ((uo.r > mx) || (uo.r < mn)) ? 2 : 0;        // :70
 }
+#else
+// A double's bits as an integer whose signed order is the double's order
+// (negative values have their magnitude bits flipped); its own inverse.
+__device__ __forceinline__ long long ord_key(double x) {
+    const long long b = __double_as_longlong(x);
+    return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ double key_val(long long k) {
+    return __longlong_as_double(k ^ ((k >> 63) & 0x7fffffffffffffffLL));
+}
+
+// Fast mode: the same tests in ~9 FP64-pipe instructions instead of ~24 (each
+// double min, max and compare is one).  For rho > 0, p > 0 iff
+// rho*E - (mx^2 + my^2)/2 > 0, so positivity needs no reciprocal; the DMP
+// bounds are the integer min and max of the densities' order keys, and the
+// bound test compares keys.  The decisions are the exact form's except where
+// p is within rounding of 0, or a density of Uin is NaN (which fmin/fmax
+// would skip).
+__device__ __forceinline__ int mood_uout_part(const Cell& uo, const double* __restrict__ uin, int nx,
+                                              const GridGeom& g) {
+    if (le_zero_or_nan(uo.r)) return 1;
+    const double ke2 = uo.mx * uo.mx + uo.my * uo.my;
+    if (!(uo.r * uo.e - 0.5 * ke2 > 0.)) return 1;     // p <= 0 or NaN
+    if (!g.dmp) return 0;
+    const size_t row = (size_t)4 * nx;
+    const long long c = ord_key(__ldg(uin)), l = ord_key(__ldg(uin - 4)), r = ord_key(__ldg(uin + 4));
+    const long long b = ord_key(__ldg(uin - row)), t = ord_key(__ldg(uin + row));
+    const long long mn = llmin(llmin(llmin(llmin(c, l), b), t), r);
+    const long long mx = llmax(llmax(llmax(llmax(c, l), b), t), r);
+    const double Mm = key_val(mx) - key_val(mn);
+    if (!(Mm > g.dx * g.dx * g.dx)) return 0;          // plateau, :68
+    const long long k = ord_key(uo.r);
+    return (k > mx || k < mn) ? 2 : 0;                 // :70
+}
+#endif
 
 __device__ __forceinline__ bool mood_shock_part(const double* __restrict__ uin, int nx, const GridGeom& g) {
     const size_t row = (size_t)4 * nx;
