@@ -246,6 +246,55 @@ __device__ __forceinline__ void hllc(const double* ul, const double* ur, double*
     for (int k = 0; k < 4; k++) F[k] = Fk[k] + S * (st[k] * dStar - u[k]);
 }
 
+#if !GPM_EXACT
+// Fast mode: hllc's arithmetic with the branches turned into selects.  Every
+// lane evaluates the star state, and the selects keep what hllc's branch
+// would have returned (the physical flux of the chosen side when the star
+// state is not used), so the flux is hllc's for admissible states.  Returns
+// false, with F undefined, when either state is inadmissible.  Without
+// branches the solves of a face's Gauss points can be scheduled together.
+template <int DIR>
+__device__ __forceinline__ bool hllc_select(const double* ul, const double* ur, double* F) {
+    const double rr = gpm_fast_rcp(ul[0] * ur[0]);
+    const Prim L = c2p<DIR>(ul, ur[0] * rr);
+    const Prim R = c2p<DIR>(ur, ul[0] * rr);
+    const double SL = fmin(L.vn - L.c, R.vn - R.c);
+    const double SR = fmax(L.vn + L.c, R.vn + R.c);
+    const double numerL = SL - L.vn, numerR = SR - R.vn;
+    double uStar = ul[0] * L.vn * numerL - ur[0] * R.vn * numerR;
+    uStar = (R.p - L.p) + uStar;
+    const double aL = ul[0] * numerL, aR = ur[0] * numerR;
+    uStar = uStar * gpm_fast_rcp(aL - aR);
+    const bool left = (SL < 0.) && (uStar >= 0.);
+    const bool right = (uStar < 0.) && (SR >= 0.);
+    const bool useL = (SL >= 0.) || left;  // whose physical flux hllc returns or corrects
+    double u[4];
+#pragma unroll
+    for (int k = 0; k < 4; k++) u[k] = useL ? ul[k] : ur[k];
+    Prim s;
+    s.vn = useL ? L.vn : R.vn;
+    s.vt = useL ? L.vt : R.vt;
+    s.p = useL ? L.p : R.p;
+    s.ir = useL ? L.ir : R.ir;
+    const double S = left ? SL : SR;
+    const double a = left ? aL : aR;
+    double Fk[4];
+    phys_flux<DIR>(u, s, Fk);
+    double st[4];
+    st[0] = 1.;
+    st[DIR == 0 ? 1 : 2] = uStar;
+    st[DIR == 0 ? 2 : 1] = s.vt;
+    const double den = S - uStar;
+    const double inv = gpm_fast_rcp(a * den);
+    const double dStar = a * a * inv;
+    st[3] = u[3] * s.ir + (uStar - s.vn) * (uStar + s.p * den * inv);
+    const bool star = left || right;
+#pragma unroll
+    for (int k = 0; k < 4; k++) F[k] = star ? Fk[k] + S * (st[k] * dStar - u[k]) : Fk[k];
+    return L.adm && R.adm;
+}
+#endif
+
 // The same primitive recovery, physical flux and HLLC with the direction a
 // runtime value (0: x, 1: y): every FP64 expression is the one hllc<DIR>
 // evaluates, only the choice of normal and tangential components is a select,
@@ -471,6 +520,22 @@ template <int DIR, int NGP>
 __device__ __forceinline__ void quad_flux(const double (*uL)[4], const double (*uR)[4], const double* gw, double* F,
                                           int nflux = 100) {
     double acc[4];
+#if !GPM_EXACT
+    if (nflux == 100) {  // HLLC without branches; NaN flux at an inadmissible Gauss point
+        bool adm = true;
+#pragma unroll
+        for (int g = 0; g < NGP; g++) {
+            double Fg[4];
+            adm = hllc_select<DIR>(uL[g], uR[g], Fg) && adm;
+#pragma unroll
+            for (int k = 0; k < 4; k++) acc[k] = (g == 0) ? Fg[k] * gw[0] : acc[k] + Fg[k] * gw[g];
+        }
+        const double nan = __longlong_as_double(0x7ff8000000000000LL);
+#pragma unroll
+        for (int k = 0; k < 4; k++) F[k] = adm ? acc[k] : nan;
+        return;
+    }
+#endif
 #pragma unroll
     for (int g = 0; g < NGP; g++) {
         double Fg[4];

@@ -487,7 +487,7 @@ __device__ __forceinline__ void edge_faces(const GridGeom& g, const GpWeights& w
 }
 
 // One cell tile per block (x fastest).
-__global__ void __launch_bounds__(XT * XY) k_flux_xy(StageArgs a, const __grid_constant__ GpWeights w, int tiles_x) {
+__global__ void __launch_bounds__(XT * XY, 2) k_flux_xy(StageArgs a, const __grid_constant__ GpWeights w, int tiles_x) {
     extern __shared__ __align__(16) unsigned char xy_raw[];
     XySmem& sm = *reinterpret_cast<XySmem*>(xy_raw);
     const int by = blockIdx.x / tiles_x, bx = blockIdx.x - by * tiles_x;
@@ -522,7 +522,7 @@ __device__ __forceinline__ bool mbar_wait(unsigned long long* bar, uint32_t pari
     return false;
 }
 
-__global__ void __launch_bounds__(XT * XY) k_flux_xy_tma(StageArgs a, const __grid_constant__ GpWeights w,
+__global__ void __launch_bounds__(XT * XY, 2) k_flux_xy_tma(StageArgs a, const __grid_constant__ GpWeights w,
                                                          const __grid_constant__ CUtensorMap tm, int tiles_x) {
     extern __shared__ __align__(1024) unsigned char xy_raw[];
     XySmem& sm = *reinterpret_cast<XySmem*>(xy_raw);
