@@ -394,6 +394,7 @@ struct XySmem {
     Cell tile[XY + 5][XT + 5];
     double left[XY][XT][XS];    // left-face states of cells l0+1 .. l0+XT
     double bottom[XY][XT][XS];  // bottom-face states of rows n0+1 .. n0+XY
+    double top[XY][XT][XS];     // each cell's own top-face states, parked during its x-face solve
 };
 
 // staged: the halo tile is already in sm.tile (TMA); otherwise load it here.
@@ -423,6 +424,7 @@ __device__ __forceinline__ void xy_tile(const GridGeom& g, const GpWeights& w, c
         }
         if (tx > 0) publish(sm.left[ty][tx - 1], xs.lo);
         if (ty > 0) publish(sm.bottom[ty - 1][tx], ys.lo);
+        publish(sm.top[ty][tx], ys.hi);
     }
     // the extra column (left states of cells l0+XT) and row (bottom states of n0+XY)
     if (ty == XY - 1 && l <= g.lf + 1 && n0 + XY <= g.nf + 1) {
@@ -457,13 +459,17 @@ __device__ __forceinline__ void xy_tile(const GridGeom& g, const GpWeights& w, c
         st_cell(fx + 4 * cidx(g, l, n), Cell{F[0], F[1], F[2], F[3]});
     }
     if (l <= g.lf && n <= g.nf) {  // y face between (l,n) and (l,n+1)
-        double uR[3][4], F[4];
+        double uL[3][4], uR[3][4], F[4];
         const double* src = sm.bottom[ty][tx];
+        const double* own = sm.top[ty][tx];
 #pragma unroll
         for (int gp = 0; gp < 3; gp++)
 #pragma unroll
-            for (int k = 0; k < 4; k++) uR[gp][k] = src[4 * gp + k];
-        quad_flux<1, 3>(ys.hi, uR, w.gw, F);
+            for (int k = 0; k < 4; k++) {
+                uL[gp][k] = own[4 * gp + k];
+                uR[gp][k] = src[4 * gp + k];
+            }
+        quad_flux<1, 3>(uL, uR, w.gw, F);
         st_cell(fy + 4 * cidx(g, l, n), Cell{F[0], F[1], F[2], F[3]});
     }
 }
