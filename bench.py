@@ -178,9 +178,9 @@ def measured_peaks():
 
 # DRAM bytes per face of one launch of the fast two-direction face kernel
 # (k_flux_xy_tma) on the 2048^2 Sedov first pass, from one ncu capture of this
-# workload: dram__bytes_read.sum + dram__bytes_write.sum = 135.71 MB + 208.22 MB
+# workload: dram__bytes_read.sum + dram__bytes_write.sum = 136.13 MB + 208.49 MB
 # over 8,392,704 faces.  A constant of that capture, not a live measurement.
-DRAM_BYTES_PER_FACE_NCU = 40.98
+DRAM_BYTES_PER_FACE_NCU = 41.06
 
 
 def cpu_oracle_rate(n, steps, threads):

@@ -1346,13 +1346,14 @@ __device__ __forceinline__ double cell_dt(const Cell& u, double dx, double dy) {
     return 1.0 / (1.0 / (dx / (fabs(vx) + c)) + 1.0 / (dy / (fabs(vy) + c)));
 }
 #else
-// Fast mode: dx*dy / ((|u|+c)*dy + (|v|+c)*dx) with Newton reciprocals, equal
-// to the form above up to rounding (a NaN or non-positive cell still gives NaN
-// or a non-positive value, which the reduction skips).
+// Fast mode: dx*dy / ((|u|+c)*dy + (|v|+c)*dx) with Newton reciprocals and
+// the fast square root, equal to the form above up to rounding (a NaN or
+// non-positive cell still gives NaN or a non-positive value, which the
+// reduction skips).
 __device__ __forceinline__ double cell_dt(const Cell& u, double dx, double dy) {
     const double ir = gpm_fast_rcp(u.r);
     const double vx = u.mx * ir, vy = u.my * ir;
-    const double c = sqrt(GPM_GAMMA * pressure_ir(u, ir) * ir);
+    const double c = gpm_fast_sqrt(GPM_GAMMA * pressure_ir(u, ir) * ir);
     return dx * dy * gpm_fast_rcp((fabs(vx) + c) * dy + (fabs(vy) + c) * dx);
 }
 #endif
