@@ -1,8 +1,10 @@
 // physics.cuh -- device physics of the GP-MOOD step: pressure, HLLC, GP dot
 // products, MOOD detection.  Included by stage_kernels.cu, which is compiled
 // twice: GPM_EXACT=1 with --fmad=false (every expression rounds exactly like
-// the reference's x86-64 build) and GPM_EXACT=0 with FMA contraction and
-// reciprocal reuse.
+// the reference's x86-64 build) and GPM_EXACT=0 with FMA contraction,
+// reciprocal reuse, Newton reciprocals and square roots from the hardware
+// approximations (fast_rcp.cuh), division-free DETECTION tests and, in the
+// first pass, an HLLC with selects instead of branches.
 //
 // Reference routines: physics.f90:9-75,132-143 (Flux, c2p_local, pressure),
 // mod_HLLC.f90:11-169 (HLLC_Flux), mod_GP_MOOD.f90:58-65 (dot products),
