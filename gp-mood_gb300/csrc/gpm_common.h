@@ -153,10 +153,8 @@ struct KernelTable {
     void (*bc)(const GridGeom& g, double* u, const DevScalars* sc, int stage, cudaStream_t s);
     int (*flux_all)(const StageArgs& a, const GpWeights& w, cudaStream_t s);  // returns the launches made
     void (*update_detect)(const StageArgs& a, const GpWeights& w, int cur, cudaStream_t s);
-    void (*mood_mark)(const StageArgs& a, int cur, int max_trb, cudaStream_t s);
+    // the faces of the listed cells tlist[cur] at their current orders (the gate's fix-up)
     void (*mood_faces)(const StageArgs& a, const GpWeights& w, int cur, int max_trb, cudaStream_t s);
-    void (*mood_cells)(const StageArgs& a, const GpWeights& w, int cur, int max_trb, unsigned pass_id,
-                       cudaStream_t s);
     void (*combine)(const GridGeom& g, const double* x, double* y, double a, double b, int with_cfl,
                     DevScalars* sc, cudaStream_t s);
     void (*cfl)(const GridGeom& g, const double* u, DevScalars* sc, cudaStream_t s);

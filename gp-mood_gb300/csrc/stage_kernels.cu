@@ -7,15 +7,17 @@
 //
 // One stage (Forward_Euler, gp-mood-code/mod_FE.f90:20-190) runs as:
 //   k_bc_x / k_bc_y       Boundary_C(Uin)                      BC.f90:10-421
-//   k_flux_tile<x|y>      every face: GP recon + HLLC + quadrature, stored
-//                         (the first MOOD pass, mod_FE.f90:73-145)
+//   k_flux_xy_tma         every face: GP recon + HLLC + quadrature, stored
+//   (k_flux_tile<x|y>)    (the first MOOD pass, mod_FE.f90:73-145); fast mode
+//                         both directions per tile, exact mode one per launch
 //   k_update_detect       Uout = Uin + flux differences, DETECTION on every
-//                         cell, troubled cells stream-compacted into a list
-//   while the list is not empty (the MOOD loop, mod_FE.f90:69-174):
-//     k_mood_mark         order cascade 5->3->1 of the troubled cells
-//     k_mood_faces        recompute the 4 faces of each troubled cell
-//     k_mood_cells        recompute Uout of the 5-point cross of each
-//                         troubled cell, re-run DETECTION there -> next list
+//                         cell, troubled cells (order already lowered 5->3->1)
+//                         compacted into a list
+//   k_mood_loop           while the list is not empty (the MOOD loop,
+//                         mod_FE.f90:69-174), in one cooperative launch:
+//                         recompute the 4 faces of each troubled cell, then
+//                         Uout of its 5-point cross with DETECTION there ->
+//                         next list
 //   k_bc_x / k_bc_y       Boundary_C(Uout)
 //   k_combine             SSP-RK3 combination (mod_SSP_RK3.f90:28,33), with
 //                         the next step's Setdt reduction fused into the last
@@ -740,16 +742,6 @@ void launch_update_detect(const StageArgs& a, const GpWeights& w, int cur, cudaS
 
 constexpr int LIST_CTAS_PER_SM = 4;
 
-// Start of a host-driven MOOD pass: count the listed cells (their orders
-// were lowered when they were listed) and empty the next list.
-__global__ void k_mood_mark(StageArgs a, int cur) {
-    const int nt = a.sc->ntrb[cur];
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
-        atomicAdd(&a.sc->detected_step, (unsigned long long)nt);
-        a.sc->ntrb[cur ^ 1] = 0;
-    }
-}
-
 // One face of the face list at its current order (min of the two cells),
 // with stencils read straight from global memory.
 template <int DIR, int NP, int NGP>
@@ -950,41 +942,6 @@ __global__ void __launch_bounds__(128) k_mood_faces(StageArgs a, const __grid_co
         if (dir == 0) face_gp_any<0>(a, w, side == 0 ? c - 1 : c, gp, f);
         else face_gp_any<1>(a, w, side == 0 ? c - a.g.nx : c, gp, f);
     });
-}
-
-__global__ void __launch_bounds__(256) k_mood_cells(StageArgs a, const __grid_constant__ GpWeights w, int cur,
-                                                    unsigned pass_id) {
-    const GridGeom& g = a.g;
-    const int nt = a.sc->ntrb[cur];
-    const double qx = a.sc->qx, qy = a.sc->qy;
-    const int nxt = cur ^ 1;
-    const int total = 5 * nt;
-    const int stride = gridDim.x * blockDim.x;
-    // Round the trip count up to a multiple of the stride so whole warps reach
-    // list_append together.
-    const int lim = ((total + stride - 1) / stride) * stride;
-    const int st = pack_tid();
-    for (int base = 0; base < lim; base += stride) {
-        const int i = base + st;
-        bool trb = false;
-        int cval = 0;
-        if (i < total) {
-            const size_t t = (size_t)a.tlist[cur][i / 5];
-            const int k = i % 5;
-            const size_t c = k == 0 ? t - g.nx : k == 1 ? t - 1 : k == 2 ? t : k == 3 ? t + 1 : t + g.nx;
-            const int l = (int)(c % (size_t)g.nx) - 3, n = (int)(c / (size_t)g.nx) - 3;
-            const bool interior = l >= 1 && l <= g.lf && n >= 1 && n <= g.nf;
-            if (interior && atomicExch(&a.stamp[c], pass_id) != pass_id) {
-                const Cell uo = cell_update(g, a.uin, a.fx, a.fy, c, qx, qy);
-                st_cell(a.uout + 4 * c, uo);
-                if (a.order[c] > 1) trb = mood_troubled(uo, a.uin + 4 * c, g.nx, g, w.d2x, w.d2y);
-                else if (inadmissible(uo)) atomicOr(&a.sc->status, GPM_STATUS_NAN);
-                cval = (int)c;
-            }
-        }
-        if (trb) cascade_order(&a.order[cval]);
-        list_append(trb, a.tlist[nxt], &a.sc->ntrb[nxt], cval);
-    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1288,9 +1245,6 @@ static int list_grid(int max_items, int threads) {
     return need < 1 ? 1 : (need < cap ? need : cap);
 }
 
-void launch_mood_mark(const StageArgs& a, int cur, int max_trb, cudaStream_t s) {
-    k_mood_mark<<<list_grid(max_trb, 256), 256, 0, s>>>(a, cur);
-}
 
 void launch_mood_faces(const StageArgs& a, const GpWeights& w, int cur, int max_trb, cudaStream_t s) {
     const int gr = list_grid(4 * max_trb, 128);
@@ -1303,10 +1257,6 @@ void launch_mood_faces(const StageArgs& a, const GpWeights& w, int cur, int max_
     }
 }
 
-void launch_mood_cells(const StageArgs& a, const GpWeights& w, int cur, int max_trb, unsigned pass_id,
-                       cudaStream_t s) {
-    k_mood_cells<<<list_grid(5 * max_trb, 256), 256, 0, s>>>(a, w, cur, pass_id);
-}
 
 // The gate's extras repair (optional): a gated cell whose update from the
 // uniform first pass (every face at mord, already stored) passes DETECTION is
@@ -1472,10 +1422,9 @@ void launch_dt_finalize(const GridGeom& g, DevScalars* sc, double dtfinal, cudaS
 __global__ void k_advance_t(DevScalars* sc) { sc->t = sc->t + sc->dt; }  // main.f90:160
 void launch_advance_t(DevScalars* sc, cudaStream_t s) { k_advance_t<<<1, 1, 0, s>>>(sc); }
 
-const KernelTable table = {launch_bc,          launch_flux_all,   launch_update_detect, launch_mood_mark,
-                           launch_mood_faces,  launch_mood_cells, launch_combine,       launch_cfl,
-                           launch_dt_finalize, launch_advance_t,  launch_mood_loop,     launch_lincomb,
-                           launch_gate_repair};
+const KernelTable table = {launch_bc,          launch_flux_all,  launch_update_detect, launch_mood_faces,
+                           launch_combine,     launch_cfl,       launch_dt_finalize,   launch_advance_t,
+                           launch_mood_loop,   launch_lincomb,   launch_gate_repair};
 
 }  // namespace GPM_NS
 
