@@ -237,6 +237,38 @@ def test_inadmissible_state_is_caught_and_reported(pkg, oracle, bad):
     assert bad_cells.any() and bad_cells.sum() < 50  # local, not spread over the grid
 
 
+@pytest.mark.parametrize("bad", ["negative_pressure", "nan_density"])
+def test_fast_mode_inadmissible_state_stays_local(pkg, oracle, bad):
+    """The fast first pass solves HLLC with selects and gives an inadmissible
+    Gauss point a NaN flux (not the reference's 1/(vx-vx)): the planted cell
+    still ends at order 1, status bit 0 reports it, the non-finite cells are
+    the exact mode's, and every other cell agrees with the exact mode to
+    1e-12."""
+    ic, lf, nf, kn = CASES["rp2d3"]
+    p = _oracle_params(oracle, lf, nf, kn)
+    U = oracle.initial_condition(p, ic)
+    dt = oracle.setdt(p, U, p.tmax)
+    j, i = 4 + 20, 4 + 30
+    if bad == "negative_pressure":
+        U[j, i, 3] = 0.5 * (U[j, i, 1] ** 2 + U[j, i, 2] ** 2) / U[j, i, 0] - 1.0
+    else:
+        U[j, i, 0] = np.nan
+    res = {}
+    for name, mode in (("exact", pkg.FP_EXACT), ("fast", pkg.FP_FAST)):
+        with _solver(pkg, lf, nf, mode, kn) as s:
+            out = np.empty_like(U)
+            s.time_stepping(U, out, 0.0, dt)
+            res[name] = (out, s.counters().status_flags, s.orders())
+    (ue, fe, oe), (uf, ff, of) = res["exact"], res["fast"]
+    assert ff & 1 and of[j - 4, i - 4] == 1
+    bad_e = ~np.isfinite(ue[4:-4, 4:-4]).all(axis=-1)
+    bad_f = ~np.isfinite(uf[4:-4, 4:-4]).all(axis=-1)
+    assert np.array_equal(bad_e, bad_f) and bad_f.sum() < 50
+    good = ~bad_f
+    a, b = ue[4:-4, 4:-4][good], uf[4:-4, 4:-4][good]
+    assert np.abs(a - b).sum() <= 1e-12 * np.abs(a).sum()
+
+
 @pytest.mark.parametrize("bc,lx,ly", [(19, 9., 1.), (201, 1.5, 1.5), (301, 1.5, 1.5), (401, 6., 1.), (402, 0.25, 1.),
                                       (403, 1., 1.)])
 def test_other_boundary_types_step_like_the_oracle(pkg, oracle, bc, lx, ly):
