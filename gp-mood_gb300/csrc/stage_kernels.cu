@@ -304,10 +304,11 @@ __device__ __forceinline__ void face_global(const GridGeom& g, const GpWeights& 
 // 13-point stencil (GpOrbit): 16 operations form the components, 32 give the
 // six x-face states and 32 the six y-face states, per variable -- 80 FP64
 // operations for 12 states, against 128 when each face gathers its two states
-// on its own.  A cell keeps its right and top states in registers and passes
-// its left and bottom states to its neighbours through shared memory; then
-// every thread solves the x face and the y face of which its cell is the low
-// side.  Tiles own the interior cells (l0..l0+XT-1, n0..n0+XY-1), l0, n0 >= 1;
+// on its own.  A cell passes its left and bottom states to its neighbours
+// through shared memory, keeps its right states in registers and parks its
+// top states in shared memory too (registers for the three Gauss points'
+// Riemann solves, which run together); then every thread solves the x face
+// and the y face of which its cell is the low side.  Tiles own the interior cells (l0..l0+XT-1, n0..n0+XY-1), l0, n0 >= 1;
 // one extra column (left states) and row (bottom states) is computed by two
 // warps.  The faces whose low cell is a ghost -- x faces (0,n), y faces (l,0)
 // -- are 32-face edge items computed face by face (edge_faces).
